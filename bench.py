@@ -1,0 +1,328 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 screen funnel (candidates/s on one generation).
+
+Workload (one "step" = one generation's screen): 2.65e9 candidates, 64 seeded
+elites, the reference's committed v3 surrogate (161 coefficients), top 256,
+T = 4 splitmix64 streams (the reference CI's --threads), sigma 0.12, jump
+0.02, immigrants 0.01, seed 7. Synthetic seeded inputs; no dataset.
+
+  value  device-resident: elites on the GPU, survivors stay on the GPU; CUDA
+         events on the launch stream around each step; L2 flushed between steps
+  e2e    the same metric through the C ABI's host-buffer call (csx_screen):
+         H2D of the elites and D2H of the survivors inside the timed region
+  roofline  the persistent screen kernel against the measured splitmix64 and
+         integer-issue rates of this GPU (the path is integer-issue bound)
+  cpu_baseline  the C restatement of the Zig screen (oracle/) on this host's
+         cores, T = 4 as the reference CI, on a bounded prefix sample
+
+`--impl reference` times the reference's CPU implementation of the path (the
+restatement: Zig is not available) on the same workload, rank 0 only.
+N > 1 GPUs run independent islands (one seed each, like the reference's CI
+shards): weak scaling, no collective on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+LAMBDA = 2_650_000_000
+KEEP = 256
+THREADS = 4
+SEED = 7
+N_ELITES = 64
+# Algorithmic 32-bit lane-ops per candidate: 61.75 splitmix64 draws x 20 +
+# 29 genes x 5 + 181 FMA x 2 ("Roofline").
+LANE_OPS_PER_CAND = 1760.0
+DRAWS_PER_CAND = 61.75
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--lambda", dest="lam", type=int, default=LAMBDA)
+    ap.add_argument("--threads", type=int, default=THREADS)
+    ap.add_argument("--keep", type=int, default=KEEP)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), \
+        int(os.environ.get("LOCAL_RANK", 0))
+
+
+def workload_config(args, n):
+    return {"workload": f"screen generation: lambda={args.lam} candidates, {N_ELITES} seeded elites, "
+                        f"committed v3 surrogate (161 coefficients), top-{args.keep}, "
+                        f"T={args.threads} RNG streams" + (f", {n} islands" if n > 1 else ""),
+            "lambda": args.lam, "keep": args.keep, "threads": args.threads, "elites": N_ELITES,
+            "surrogate": "state/surrogate.txt (v3, 161)", "sigma": 0.12, "jump_p": 0.02, "imm_p": 0.01,
+            "seed": SEED, "l2": "flushed between steps (256 MiB write); inputs are a 10 KB elite pool",
+            "parallelism": f"islands{n}" if n > 1 else "single"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev_index):
+        self.dev = dev_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) >= 9:
+                rows.append(p)
+        os.remove(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows),
+                "power_w_max": max((float(r[3]) for r in rows if r[3].replace(".", "").isdigit()),
+                                   default=None)}
+
+
+def cpu_baseline(args, seconds):
+    """The oracle (C restatement of src/screen.zig) at T streams, T threads, on a
+    prefix sample of the workload sized to about `seconds` of CPU time."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    from codec_arena_gb300 import workloads as wl
+
+    el = wl.seeded_elites(N_ELITES)
+    m = oracle.model_from_compact(wl.surrogate_161())
+    T = args.threads
+    lam = 400_000
+    t0 = time.perf_counter()
+    oracle.screen(oracle.cfg(lam, args.keep, SEED, threads=T), m, el, cpu_threads=T)
+    dt = time.perf_counter() - t0
+    lam = int(min(args.lam, max(lam, lam * seconds / max(dt, 1e-6))))
+    lam -= lam % T
+    t0 = time.perf_counter()
+    _, screened = oracle.screen(oracle.cfg(lam, args.keep, SEED, threads=T), m, el, cpu_threads=T)
+    dt = time.perf_counter() - t0
+    return {"value": screened / dt, "unit": "candidates/s", "cores": T, "kind": "port",
+            "sample": f"first {lam // T} candidates of each of the T={T} streams "
+                      f"({lam} candidates, {dt:.1f} s), C restatement built -O3 -ffp-contract=off",
+            "host_threads_available": os.cpu_count()}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    steps, warm = args.steps, args.warmup
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    from codec_arena_gb300 import workloads as wl
+
+    el = wl.seeded_elites(N_ELITES)
+    m = oracle.model_from_compact(wl.surrogate_161())
+    T = args.threads
+    # bounded sample per step: the T-stream prefix that takes ~2 s on T threads
+    lam = 400_000
+    t0 = time.perf_counter()
+    oracle.screen(oracle.cfg(lam, args.keep, SEED, threads=T), m, el, cpu_threads=T)
+    dt = time.perf_counter() - t0
+    lam = int(min(args.lam, max(lam, lam * 2.0 / max(dt, 1e-6))))
+    lam -= lam % T
+    for _ in range(warm):
+        oracle.screen(oracle.cfg(lam // 10, args.keep, SEED, threads=T), m, el, cpu_threads=T)
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        oracle.screen(oracle.cfg(lam, args.keep, SEED, threads=T), m, el, cpu_threads=T)
+        times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    v = lam * steps / tot
+    line = {"impl": "reference", "metric": "candidates/sec (screen generation, 1 GB300 host)",
+            "value": v, "unit": "candidates/s", "n_gpus": world, "steps": steps, "warmup": warm,
+            "ms_per_step": 1000 * tot / steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64/f32", "data": "synthetic (seeded)",
+            "config": workload_config(args, 1),
+            "cpu_baseline": {"value": v, "unit": "candidates/s", "cores": T, "kind": "port",
+                             "sample": f"each step: first {lam // T} candidates of each of T={T} "
+                                       f"streams ({lam} candidates) on {T} threads; Zig is not "
+                                       "available, the C restatement of src/screen.zig runs"},
+            "e2e": {"value": v, "unit": "candidates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import numpy as np
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from codec_arena_gb300 import _lib, build, screen, workloads as wl
+
+    build.build()
+    bench = ctypes.CDLL(build.BENCH_LIB)
+    bench.csx_bench_issue_rate.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+
+    el = wl.seeded_elites(N_ELITES)
+    model = screen.Model.from_compact(wl.surrogate_161())
+    seed = SEED if world == 1 else SEED * 1000003 + rank * 131  # one island per rank
+    cfg = screen.Cfg(args.lam, args.keep, seed, threads=args.threads, flags=_lib.FLAG_STAGE_TIMES)
+    d_el = torch.from_numpy(el.view(np.uint8).copy()).cuda()
+    d_out = torch.zeros(args.keep * _lib.SURVIVOR_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    d_res = torch.zeros(4, dtype=torch.int64, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    st = torch.cuda.current_stream()
+
+    def step():
+        screen.screen_device(cfg, model, d_el, d_out, d_res, stream=st)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    res = d_res.cpu().numpy()
+    assert res[2] == 0 and res[1] == args.lam, f"device result {res}"
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    screen_ms, stage = [], []
+    barrier()
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    for i in range(args.steps):
+        flush.fill_(i & 0xFF)
+        ev[i][0].record(st)
+        step()
+        ev[i][1].record(st)
+        info = screen.last_run_info()  # waits for this step's last stage
+        screen_ms.append(info["ms_screen"])
+        stage.append(info)
+    torch.cuda.synchronize()
+    barrier()
+    wall = time.perf_counter() - w0
+    clocks = sampler.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    t_dev = sum(step_ms) / 1000.0
+    if world > 1:
+        t = torch.tensor([t_dev], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_dev = float(t.item())
+    value = world * args.lam * args.steps / t_dev
+    launches = stage[-1]["launches"]
+
+    # e2e: host buffers through the C ABI (H2D elites, D2H survivors timed)
+    e2e_steps = max(1, min(3, args.steps))
+    hcfg = screen.Cfg(args.lam, args.keep, seed, threads=args.threads)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        surv, scr = screen.screen(hcfg, model, el)
+    e2e_t = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_t], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_t = float(t.item())
+    e2e = {"value": world * args.lam * e2e_steps / e2e_t, "unit": "candidates/s",
+           "h2d_bytes_per_step": int(el.nbytes + ctypes.sizeof(_lib.CsxModel) + ctypes.sizeof(_lib.CsxCfg)),
+           "d2h_bytes_per_step": int(len(surv) * _lib.SURVIVOR_DTYPE.itemsize + 32),
+           "api": "csx_screen (host buffers, synchronous)"}
+
+    if rank != 0:
+        return
+    rates = {}
+    for kind, name in ((0, "int_alu"), (1, "imad"), (2, "ffma"), (3, "splitmix64")):
+        r = ctypes.c_double(0)
+        if bench.csx_bench_issue_rate(kind, ctypes.byref(r)) == 0:
+            rates[name] = r.value
+    ms_screen = statistics.mean(screen_ms)
+    cand_s_kernel = args.lam / (ms_screen / 1000.0)
+    achieved = cand_s_kernel * LANE_OPS_PER_CAND / 1e12
+    peak = rates.get("int_alu", 0.0) / 1e12
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "screen_kernel_traffic.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get("bytes_per_launch_full_workload")
+        except Exception:
+            traffic = None
+    roofline = {
+        "bound": "int-issue", "kernel": "csx::screen_kernel<true>",
+        "achieved": achieved, "peak": peak, "unit": "Tlane-op/s",
+        "frac": achieved / peak if peak else None, "traffic": traffic,
+        "algorithmic_ops_per_candidate": LANE_OPS_PER_CAND,
+        "peak_source": "measured: integer ALU issue rate of this GPU (csx_bench_issue_rate kind 0)",
+        "splitmix64_bound": {"hashes_per_s": rates.get("splitmix64"),
+                             "achieved_hashes_per_s": cand_s_kernel * DRAWS_PER_CAND,
+                             "frac": (cand_s_kernel * DRAWS_PER_CAND / rates["splitmix64"])
+                             if rates.get("splitmix64") else None},
+        "issue_rates_measured": rates,
+        "kernel_ms_per_launch": ms_screen,
+    }
+    line = {"metric": "candidates/sec (screen generation, 1 GB300)", "value": value, "unit": "candidates/s",
+            "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
+            "ms_per_step": 1000.0 * t_dev / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64/f32", "data": "synthetic (seeded)",
+            "config": workload_config(args, world), "e2e": e2e, "roofline": roofline,
+            "clocks": clocks, "gpu_launches": int(launches * args.steps),
+            "stages_ms_last_step": {k: round(v, 4) for k, v in stage[-1].items() if k.startswith("ms_")},
+            "shape": {k: stage[-1][k] for k in ("screen_ctas", "segments", "seg_draws", "item_cands")},
+            "wall_s": wall}
+    if world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args, args.cpu_seconds)
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,201 @@
+// csx_device.cuh — device primitives of the screen funnel (sm_103a).
+//
+// One candidate of src/screen.zig:225-253 is synthesised and scored per call,
+// entirely in registers. splitmix64 (src/screen.zig:202-208) is counter based:
+// the state before draw q of stream t is seed_t + q*G, so any draw can be
+// computed directly from its position. Every use below computes only the
+// part of the 64-bit output it consumes:
+//   * parent / jump index   (next() >> 32):  hi word, final xor-shift kept
+//   * unit()  (next() >> 40): bits 63..40 are untouched by the final
+//     `z ^ (z >> 31)`, so the hi word of the second product suffices
+//   * crossover bit (next() & 1) = bit0 ^ bit31 of the low word of the second
+//     product; multiplying that low word by (2^31 + 1) moves the XOR into bit
+//     31, and the factor folds into the multiply constant: one IMUL.
+// All f32 arithmetic that reaches a gene or a score uses explicit _rn
+// intrinsics, so nothing is contracted into FMA unless written as one.
+#pragma once
+
+#include <cstdint>
+
+namespace csx {
+
+constexpr uint64_t kGolden = 0x9E3779B97F4A7C15ull;
+constexpr uint64_t kMix1 = 0xBF58476D1CE4E5B9ull;
+constexpr uint64_t kMix2 = 0x94D049BB133111EBull;
+constexpr uint32_t kMix2LoFold = static_cast<uint32_t>(kMix2) * 0x80000001u;
+constexpr int kNtot = 29;
+constexpr int kNq = 136;  // lower-triangular quad terms over the 16 legacy genes
+
+// Model in the compact triangular form used on the device.
+struct DevModel {
+    float w0;
+    float wlin[kNtot];
+    float wq[kNq];  // (i, j <= i) at i*(i+1)/2 + j  ==  Model.w_quad[i*16 + j]
+};
+
+// Per-call synthesis constants (uniform across the grid).
+struct SynthConst {
+    uint64_t ne_magic;  // Lemire fastmod constant for ne
+    uint32_t ne;        // elite count; row ne of the elite table holds 0.5s
+    uint32_t imm_thr;   // unit() < imm_p   <=>  (next() >> 40) < imm_thr
+    uint32_t jump_thr;  // unit() < jump_p  <=>  (next() >> 40) < jump_thr
+    float sigma;
+    float nsig1;  // -sigma
+    float nsig2;  // -2 sigma
+};
+
+__host__ __device__ constexpr int tri(int i, int j) { return i * (i + 1) / 2 + j; }
+
+// y = z * kMix1 where z = s ^ (s >> 30): the first half of the mixer.
+__device__ __forceinline__ uint64_t mix_a(uint64_t s) {
+    const uint64_t z = s ^ (s >> 30);
+    return z * kMix1;
+}
+
+// hi word of v = u * kMix2, u = y ^ (y >> 27). Bits 31..8 of it are bits
+// 63..40 of next(); (vh >> 8) is next() >> 40.
+__device__ __forceinline__ uint32_t draw_vh(uint64_t s) {
+    const uint64_t y = mix_a(s);
+    const uint64_t u = y ^ (y >> 27);
+    return static_cast<uint32_t>((u * kMix2) >> 32);
+}
+
+// next() >> 32.
+__device__ __forceinline__ uint32_t draw_hi(uint64_t s) {
+    const uint32_t vh = draw_vh(s);
+    return vh ^ (vh >> 31);
+}
+
+// Sign bit == next() & 1.
+__device__ __forceinline__ uint32_t draw_bitword(uint64_t s) {
+    const uint64_t y = mix_a(s);
+    const uint32_t ul = static_cast<uint32_t>(y ^ (y >> 27));
+    return ul * kMix2LoFold;
+}
+
+// x % d for 32-bit x and 1 <= d < 2^32 (Lemire, Kaser, Kurz 2019):
+// M = floor((2^64 - 1) / d) + 1, x % d = hi64((M * x mod 2^64) * d).
+__device__ __forceinline__ uint32_t fastmod_u32(uint32_t x, uint64_t M, uint32_t d) {
+    const uint64_t low = M * x;
+    const uint32_t lo = static_cast<uint32_t>(low), hi = static_cast<uint32_t>(low >> 32);
+    const uint64_t p1 = static_cast<uint64_t>(hi) * d + __umulhi(lo, d);
+    return static_cast<uint32_t>(p1 >> 32);
+}
+
+// Header of the candidate at draw position p (src/screen.zig:232-235,247-248).
+struct CandHead {
+    uint32_t ea, eb;   // parent rows
+    uint32_t jidx;     // jump gene index, 0xFF when no jump
+    float jval;        // jump value
+    bool imm;          // immigrant
+    uint32_t len;      // draws the candidate consumes: 33/35/62/64
+};
+
+__device__ __forceinline__ CandHead cand_head(const SynthConst &C, uint64_t seed_t, uint64_t p) {
+    CandHead h;
+    const uint64_t s0 = seed_t + (p + 1) * kGolden;  // state after draw p's increment
+    h.ea = fastmod_u32(draw_hi(s0), C.ne_magic, C.ne);
+    h.eb = fastmod_u32(draw_hi(s0 + kGolden), C.ne_magic, C.ne);
+    h.imm = (draw_vh(s0 + 2 * kGolden) >> 8) < C.imm_thr;
+    const uint64_t sj = s0 + (h.imm ? 32ull : 61ull) * kGolden;  // draw p+3+29 / p+3+58
+    const bool jump = (draw_vh(sj) >> 8) < C.jump_thr;
+    const uint32_t idx = draw_hi(sj + kGolden) % 29u;             // index drawn first
+    h.jval = static_cast<float>(draw_vh(sj + 2 * kGolden) >> 8) * (1.0f / 16777216.0f);
+    h.jidx = jump ? idx : 0xFFu;
+    h.len = (h.imm ? 33u : 62u) + (jump ? 2u : 0u);
+    return h;
+}
+
+// One candidate: genes in registers, score in the reference's op order
+// (src/screen.zig:97-112):
+//   lane l:  acc_l = w0 + wl_l*g_l;  sum_l = sum_{i=l..15} Wq[i][l]*(g_l*g_i)
+//   score = (((acc_0+sum_0) + (acc_1+sum_1)) + ... ) + rsum,  rsum = sum_{k>=16} wl_k*g_k
+// The strict upper triangle of Wq is +0 and g >= 0, so its terms add +0 and
+// are skipped; the first add into sum_l keeps the reference's 0 + x.
+//
+// Immigrants (src/screen.zig:235-237) run the crossover arithmetic with both
+// parents on a row of 0.5s and half-width 0.5: 0.5 + (u - 0.5) == u exactly.
+// Their unit draws are consecutive; crossover genes alternate bit and unit.
+//
+// kFastDelta: delta = fma(y, B, -c*B) with y in [1,2), c in {1,2}; -c*B is
+// exact, so this is one rounding of (y-c)*B == round((u-0.5)*2*B). Valid for
+// finite |B| <= 2^126; otherwise the two-op form is used.
+template <bool kFastDelta, bool kKeepGenes>
+__device__ __forceinline__ float synth_score(const DevModel &M, const SynthConst &C,
+                                             const float *__restrict__ el, uint64_t seed_t,
+                                             uint64_t p, const CandHead &h, float *genes) {
+    const uint64_t s0 = seed_t + (p + 1) * kGolden;
+    const uint32_t ra = h.imm ? C.ne : h.ea;
+    const uint32_t rb = h.imm ? C.ne : h.eb;
+    const float *pa = el + ra * kNtot;
+    const float *pb = el + rb * kNtot;
+    const float B = h.imm ? 0.5f : C.sigma;
+    const float nb1 = h.imm ? -0.5f : C.nsig1;
+    const float nb2 = h.imm ? -1.0f : C.nsig2;
+    const uint64_t step = h.imm ? kGolden : 2 * kGolden;
+    uint64_t su = s0 + (h.imm ? 3ull : 4ull) * kGolden;  // unit draw of gene 0
+
+    float G[16], S[16];
+    float R = 0.0f;
+#pragma unroll
+    for (int k = 0; k < kNtot; ++k) {
+        const uint32_t bw = draw_bitword(su - kGolden);  // crossover bit draw
+        const uint32_t vh = draw_vh(su);                 // unit draw
+        su += step;
+        const float *src = (static_cast<int32_t>(bw) < 0) ? pb : pa;
+        const float par = src[k];
+        const float y = __uint_as_float(((vh >> 8) & 0x7FFFFFu) | 0x3F800000u);
+        float g;
+        if (kFastDelta) {
+            const float nc = (static_cast<int32_t>(vh) < 0) ? nb1 : nb2;
+            g = __fadd_rn(par, __fmaf_rn(y, B, nc));
+        } else {
+            const float nc = (static_cast<int32_t>(vh) < 0) ? -1.0f : -2.0f;
+            g = __fadd_rn(par, __fmul_rn(__fadd_rn(y, nc), B));
+        }
+        g = fmaxf(fminf(g, 1.0f), 0.0f);  // clamp01: NaN -> 1 as minnum
+        g = (static_cast<uint32_t>(k) == h.jidx) ? h.jval : g;
+        if (kKeepGenes) genes[k] = g;
+        if (k < 16) {
+            G[k] = g;
+#pragma unroll
+            for (int l = 0; l < k; ++l)
+                S[l] = __fadd_rn(S[l], __fmul_rn(M.wq[tri(k, l)], __fmul_rn(G[l], g)));
+            S[k] = __fadd_rn(0.0f, __fmul_rn(M.wq[tri(k, k)], __fmul_rn(g, g)));
+        } else {
+            const float t = __fmul_rn(M.wlin[k], g);
+            R = (k == 16) ? __fadd_rn(0.0f, t) : __fadd_rn(R, t);
+        }
+    }
+    float r = __fadd_rn(__fadd_rn(M.w0, __fmul_rn(M.wlin[0], G[0])), S[0]);
+#pragma unroll
+    for (int l = 1; l < 16; ++l)
+        r = __fadd_rn(r, __fadd_rn(__fadd_rn(M.w0, __fmul_rn(M.wlin[l], G[l])), S[l]));
+    return __fadd_rn(r, R);
+}
+
+// Candidate-start walk: position of the next candidate after the one at p.
+// The draws at p+32 and p+61 (both possible jump tests) are computed beside
+// the immigrant test so the chain advances one hash latency per step.
+__device__ __forceinline__ uint64_t walk_step(const SynthConst &C, uint64_t seed_t, uint64_t p) {
+    const uint64_t s0 = seed_t + (p + 1) * kGolden;
+    const bool imm = (draw_vh(s0 + 2 * kGolden) >> 8) < C.imm_thr;
+    const bool ja = (draw_vh(s0 + 32 * kGolden) >> 8) < C.jump_thr;
+    const bool jb = (draw_vh(s0 + 61 * kGolden) >> 8) < C.jump_thr;
+    const bool jump = imm ? ja : jb;
+    return p + (imm ? 33u : 62u) + (jump ? 2u : 0u);
+}
+
+// Order-preserving key of a score; -0 ranks with +0 and NaN below everything.
+__device__ __forceinline__ uint32_t score_okey(float x) {
+    x = __fadd_rn(x, 0.0f);
+    const uint32_t b = __float_as_uint(x);
+    const uint32_t k = (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+    return (x != x) ? 0u : k;
+}
+
+__device__ __forceinline__ float okey_score(uint32_t k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
+}
+
+}  // namespace csx

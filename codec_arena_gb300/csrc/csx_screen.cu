@@ -1,0 +1,971 @@
+// csx_screen.cu — the GB300 screen funnel: src/screen.zig:run as a pipeline
+// of sm_103a kernels behind the C ABI of include/csx_screen.h.
+//
+// Work decomposition. The reference runs T splitmix64 streams, stream t
+// producing my_t candidates sequentially (src/screen.zig:273-297). A
+// candidate consumes 33, 35, 62 or 64 draws, so where candidate i starts in
+// its stream is only known by walking the stream. The pipeline:
+//
+//  1. walk    one thread per segment of L draws: follow the chain of
+//             candidate starts from the segment's first draw (a guess), record
+//             a checkpoint every D candidates, then follow this chain and the
+//             next segment's guess chain in tandem until they meet. Two chains
+//             that share a position coincide from there on; the first
+//             segment's chain starts at draw 0 and is the true one, so the
+//             truth is recovered segment by segment at the meeting points.
+//  2. assemble one thread per stream: turn meeting points into the true
+//             candidate range of every segment and its stream-local indices.
+//  3. scan + emit  work items of <= D candidates with known start draw and
+//             stream-local index, in (stream, index) order.
+//  4. screen  persistent CTAs pull items; each thread synthesises and scores
+//             candidates in registers; those that beat the CTA's threshold go
+//             to a shared-memory buffer that is merged into the CTA's sorted
+//             top-K list (bitonic sort). HBM sees only items and survivors.
+//  5. merge   a tree of pairwise bitonic merges reduces the CTA lists.
+//  6. regen   the K survivors are re-synthesised from (stream, draw) to
+//             recover genes and lineage; the score is re-checked bit for bit.
+//
+// The walk costs two to three hashes per candidate against ~64 for
+// synthesis. When streams are no longer than one item, steps 1-3 are skipped.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "../../include/csx_screen.h"
+#include "csx_device.cuh"
+
+namespace csx {
+
+constexpr int kThreads = 256;      // screen CTA
+constexpr int kRounds = 2;         // candidates per thread between buffer checks
+constexpr uint32_t kMaxKeep = 4096;
+constexpr uint32_t kMaxElites = 1536;
+constexpr uint64_t kLinkCap = 1ull << 26;
+constexpr uint32_t kDefaultSegCands = 32768;
+
+enum : uint32_t { kErrLink = 1u, kErrAssemble = 2u, kErrRegen = 4u, kErrItems = 8u };
+enum : uint32_t { kSegOk = 0, kSegLast = 1, kSegFail = 2 };
+
+struct Item {
+    uint64_t draw0;   // first draw of the item's first candidate
+    uint64_t idx0;    // stream-local index of that candidate
+    uint32_t stream;
+    uint32_t n;       // candidates in the item
+};
+
+// Top-K entry, ordered by (k1, k2) descending:
+//   k1 = okey(score) << 32 | ~item,  k2 = ~dcand << 32 | ddraw
+// so ties on the score go to the lower (stream, index). Zero is padding.
+struct Entry {
+    unsigned long long k1, k2;
+};
+
+struct SegRec {
+    uint64_t merge_pos;  // first draw shared by this chain and the next segment's
+    uint32_t n;          // chain candidates starting inside the segment
+    uint32_t a;          // chain candidates from the segment end to merge_pos
+    uint32_t b_next;     // next segment's chain candidates before merge_pos
+    uint32_t status;
+};
+
+struct SegOut {
+    uint64_t pos;   // draw of the first true candidate in this segment
+    uint64_t I;     // its stream-local index
+    uint64_t lo;    // its index along the segment's chain
+    uint32_t cnt;   // true candidates taken from this segment
+    uint32_t nitems;
+};
+
+struct Ctrl {
+    unsigned int next_item;
+    unsigned int gtau;  // best CTA threshold key seen so far (score okey)
+    unsigned int err;
+    unsigned int n_items;
+    unsigned long long screened;
+    unsigned long long n_out;
+};
+
+struct StreamGeom {
+    uint64_t seed, T, per, my_last, L, n_seg;
+    uint32_t C, C_last, d_log2, ckcap;
+};
+
+__device__ __forceinline__ bool better(const Entry &a, const Entry &b) {
+    return a.k1 > b.k1 || (a.k1 == b.k1 && a.k2 > b.k2);
+}
+
+__device__ __forceinline__ void seg_of(const StreamGeom &g, uint64_t s, uint64_t &t, uint32_t &c) {
+    t = s / g.C;
+    if (t > g.T - 1) t = g.T - 1;
+    c = static_cast<uint32_t>(s - t * g.C);
+}
+
+__device__ __forceinline__ uint64_t stream_seed(uint64_t seed, uint64_t t) {
+    return seed ^ (kGolden * (t + 1));  // src/screen.zig:284
+}
+
+// Split points m*D with lo < m*D < lo + cnt that have a checkpoint (m < ckcap).
+__device__ __forceinline__ void split_range(uint64_t lo, uint64_t cnt, uint32_t dl, uint32_t ckcap,
+                                            uint64_t &mmin, uint64_t &mmax) {
+    mmin = (lo >> dl) + 1;
+    mmax = (lo + cnt - 1) >> dl;
+    if (mmax > static_cast<uint64_t>(ckcap) - 1) mmax = static_cast<uint64_t>(ckcap) - 1;
+}
+
+// ---- 0. elite table ---------------------------------------------------------
+
+// (ne + 1) x 29 table, row ne = 0.5 (the immigrant row); -0.0 genes become
+// +0.0 (clamp01 of a crossover gene can then never see -0.0).
+__global__ void prep_elites_kernel(const csx_genome *__restrict__ el, int ne, float *__restrict__ tab,
+                                   unsigned long long *__restrict__ ids, unsigned int *__restrict__ tribes) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < ne * kNtot) {
+        const int r = i / kNtot, k = i - r * kNtot;
+        tab[i] = __fadd_rn(el[r].g[k], 0.0f);
+    } else if (i < (ne + 1) * kNtot) {
+        tab[i] = 0.5f;
+    }
+    if (i < ne) {
+        ids[i] = el[i].id;
+        tribes[i] = el[i].tribe;
+    }
+}
+
+// ---- 1. walk ------------------------------------------------------------------
+
+__global__ void walk_kernel(SynthConst sc, StreamGeom g, SegRec *__restrict__ recs,
+                            uint64_t *__restrict__ ck, Ctrl *__restrict__ ctrl) {
+    const uint64_t s = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (s >= g.n_seg) return;
+    uint64_t t;
+    uint32_t c;
+    seg_of(g, s, t, c);
+    const bool last_stream = t == g.T - 1;
+    const uint64_t my = last_stream ? g.my_last : g.per;
+    const uint32_t ct = last_stream ? g.C_last : g.C;
+    const uint64_t seed_t = stream_seed(g.seed, t);
+    const uint64_t b = static_cast<uint64_t>(c) * g.L, e = b + g.L;
+    uint64_t *ckp = ck + s * g.ckcap;
+    const uint64_t dmask = (1ull << g.d_log2) - 1;
+    uint64_t p = b, k = 0;
+    const uint64_t limit = (ct == 1) ? my : ~0ull;  // a lone segment starts at the truth
+    while (p < e && k < limit) {
+        if ((k & dmask) == 0) {
+            const uint64_t m = k >> g.d_log2;
+            if (m < g.ckcap) ckp[m] = p;
+        }
+        p = walk_step(sc, seed_t, p);
+        ++k;
+    }
+    SegRec r;
+    r.n = static_cast<uint32_t>(k);
+    r.a = 0;
+    r.b_next = 0;
+    if (c + 1 == ct) {
+        r.status = kSegLast;
+        r.merge_pos = p;
+        recs[s] = r;
+        return;
+    }
+    // link: this chain (at p) and the next segment's guess chain (from e)
+    uint64_t q = e, kb = 0, steps = 0;
+    r.status = kSegOk;
+    while (p != q) {
+        if (p < q) {
+            if ((k & dmask) == 0) {
+                const uint64_t m = k >> g.d_log2;
+                if (m < g.ckcap) ckp[m] = p;
+            }
+            p = walk_step(sc, seed_t, p);
+            ++k;
+        } else {
+            q = walk_step(sc, seed_t, q);
+            ++kb;
+        }
+        if (++steps > kLinkCap) {
+            r.status = kSegFail;
+            atomicOr(&ctrl->err, kErrLink);
+            break;
+        }
+    }
+    r.merge_pos = p;
+    r.a = static_cast<uint32_t>(k - r.n);
+    r.b_next = static_cast<uint32_t>(kb);
+    recs[s] = r;
+}
+
+// ---- 2. assemble ------------------------------------------------------------------
+
+__global__ void assemble_kernel(StreamGeom g, const SegRec *__restrict__ recs, SegOut *__restrict__ outs,
+                                Ctrl *__restrict__ ctrl) {
+    const uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= g.T) return;
+    const bool last_stream = t == g.T - 1;
+    const uint64_t my = last_stream ? g.my_last : g.per;
+    const uint32_t ct = last_stream ? g.C_last : g.C;
+    const uint64_t s0 = t * g.C;
+    uint64_t lo = 0, pos = 0, idx = 0;
+    bool bad = false;
+    for (uint32_t c = 0; c < ct; ++c) {
+        const SegRec r = recs[s0 + c];
+        SegOut o;
+        o.pos = pos;
+        o.I = idx;
+        o.lo = lo;
+        o.cnt = 0;
+        o.nitems = 0;
+        if (r.status == kSegFail) bad = true;
+        const uint64_t hi = (r.status == kSegLast) ? r.n : static_cast<uint64_t>(r.n) + r.a;
+        if (!bad && idx < my && hi > lo) {
+            uint64_t cnt = hi - lo;
+            if (cnt > my - idx) cnt = my - idx;
+            uint64_t mmin, mmax;
+            split_range(lo, cnt, g.d_log2, g.ckcap, mmin, mmax);
+            o.cnt = static_cast<uint32_t>(cnt);
+            o.nitems = 1 + (mmax >= mmin ? static_cast<uint32_t>(mmax - mmin + 1) : 0u);
+            idx += cnt;
+        }
+        outs[s0 + c] = o;
+        if (r.status == kSegOk) {
+            if (hi >= lo) {  // the truth reaches the meeting point along this chain
+                lo = r.b_next;
+                pos = r.merge_pos;
+            } else {         // the truth joined this chain after it met the next one
+                lo = r.b_next + (lo - hi);
+            }
+        }
+    }
+    if (idx != my) atomicOr(&ctrl->err, kErrAssemble);
+}
+
+// ---- 3. scan + emit ---------------------------------------------------------------
+
+// Exclusive scan of SegOut::nitems by one CTA of 1024 threads (contiguous
+// chunk per thread, then a block scan of the chunk sums).
+__global__ void __launch_bounds__(1024) scan_kernel(const SegOut *__restrict__ outs, uint64_t n,
+                                                    uint32_t *__restrict__ off, Ctrl *__restrict__ ctrl,
+                                                    uint64_t items_cap) {
+    __shared__ unsigned long long wsum[32];
+    const uint32_t tid = threadIdx.x;
+    const uint64_t per = (n + blockDim.x - 1) / blockDim.x;
+    const uint64_t b = tid * per, e = min(n, b + per);
+    unsigned long long local = 0;
+    for (uint64_t i = b; i < e; ++i) local += outs[i].nitems;
+    // block exclusive scan of `local`
+    unsigned long long v = local;
+    const int lane = tid & 31, w = tid >> 5;
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += u;
+    }
+    if (lane == 31) wsum[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        unsigned long long x = lane < static_cast<int>(blockDim.x >> 5) ? wsum[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long u = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += u;
+        }
+        wsum[lane] = x;
+    }
+    __syncthreads();
+    unsigned long long base = (w > 0 ? wsum[w - 1] : 0ull) + v - local;
+    for (uint64_t i = b; i < e; ++i) {
+        off[i] = static_cast<uint32_t>(base);
+        base += outs[i].nitems;
+    }
+    if (tid == blockDim.x - 1) {
+        if (base > items_cap || base >= 0xFFFFFFFFull) {
+            atomicOr(&ctrl->err, kErrItems);
+            base = 0;
+        }
+        ctrl->n_items = static_cast<unsigned int>(base);
+    }
+}
+
+__global__ void emit_kernel(StreamGeom g, const SegOut *__restrict__ outs, const uint32_t *__restrict__ off,
+                            const uint64_t *__restrict__ ck, Item *__restrict__ items,
+                            const Ctrl *__restrict__ ctrl) {
+    const uint64_t s = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (s >= g.n_seg) return;
+    const SegOut o = outs[s];
+    if (o.cnt == 0 || (ctrl->err & kErrItems)) return;
+    uint64_t t;
+    uint32_t c;
+    seg_of(g, s, t, c);
+    const uint64_t *ckp = ck + s * g.ckcap;
+    uint32_t j = off[s];
+    uint64_t cur_lo = o.lo, cur_pos = o.pos, cur_i = o.I;
+    const uint64_t end = o.lo + o.cnt;
+    uint64_t mmin, mmax;
+    split_range(o.lo, o.cnt, g.d_log2, g.ckcap, mmin, mmax);
+    for (uint64_t m = mmin; m <= mmax; ++m) {
+        const uint64_t nxt = m << g.d_log2;
+        Item it;
+        it.draw0 = cur_pos;
+        it.idx0 = cur_i;
+        it.stream = static_cast<uint32_t>(t);
+        it.n = static_cast<uint32_t>(nxt - cur_lo);
+        items[j++] = it;
+        cur_i += nxt - cur_lo;
+        cur_lo = nxt;
+        cur_pos = ckp[m];
+    }
+    Item it;
+    it.draw0 = cur_pos;
+    it.idx0 = cur_i;
+    it.stream = static_cast<uint32_t>(t);
+    it.n = static_cast<uint32_t>(end - cur_lo);
+    items[j] = it;
+}
+
+// Streams no longer than one item: one item per stream, starting at draw 0.
+__global__ void stream_items_kernel(StreamGeom g, Item *__restrict__ items, Ctrl *__restrict__ ctrl) {
+    const uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t == 0) ctrl->n_items = static_cast<unsigned int>(g.T);
+    if (t >= g.T) return;
+    Item it;
+    it.draw0 = 0;
+    it.idx0 = 0;
+    it.stream = static_cast<uint32_t>(t);
+    it.n = static_cast<uint32_t>(t == g.T - 1 ? g.my_last : g.per);
+    items[t] = it;
+}
+
+// ---- 4. screen ----------------------------------------------------------------
+
+struct ScreenArgs {
+    DevModel m;
+    SynthConst sc;
+    uint64_t seed;
+    const float *el;  // (ne + 1) x 29
+    const Item *items;
+    Ctrl *ctrl;
+    Entry *lists;     // gridDim.x x kpad
+    uint32_t keep, kpad, sort_n, buf_cap;
+};
+
+// Bitonic sort of E[0..n) (n a power of two), best entry first.
+__device__ void cta_sort_desc(Entry *E, uint32_t n) {
+    for (uint32_t size = 2; size <= n; size <<= 1) {
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            for (uint32_t i = threadIdx.x; i < (n >> 1); i += blockDim.x) {
+                const uint32_t lo = 2 * i - (i & (stride - 1));
+                const uint32_t hi = lo + stride;
+                const bool desc = (lo & size) == 0;
+                const Entry a = E[lo], b = E[hi];
+                if (desc ? better(b, a) : better(a, b)) {
+                    E[lo] = b;
+                    E[hi] = a;
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+template <bool kFastDelta>
+__global__ void __launch_bounds__(kThreads) screen_kernel(const __grid_constant__ ScreenArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Entry *E = reinterpret_cast<Entry *>(smem_raw);
+    float *el = reinterpret_cast<float *>(E + A.sort_n);
+    __shared__ unsigned int s_buf_n;
+    __shared__ unsigned long long s_t1, s_t2;
+    __shared__ float s_ts;
+
+    const uint32_t tid = threadIdx.x;
+    for (uint32_t i = tid; i < A.sort_n; i += kThreads) E[i] = Entry{0ull, 0ull};
+    for (uint32_t i = tid; i < (A.sc.ne + 1) * kNtot; i += kThreads) el[i] = A.el[i];
+    if (tid == 0) {
+        s_buf_n = 0;
+        s_t1 = 0;
+        s_t2 = 0;
+        s_ts = -INFINITY;
+    }
+    const unsigned int n_items = *reinterpret_cast<volatile unsigned int *>(&A.ctrl->n_items);
+    __syncthreads();
+
+    Entry *buf = E + A.kpad;
+    uint32_t item = atomicAdd(&A.ctrl->next_item, 1u);
+    bool valid = item < n_items;
+    uint64_t seed_t = 0, p = 0;
+    uint32_t left = 0, dcand = 0, ddraw = 0;
+    if (valid) {
+        const Item it = A.items[item];
+        seed_t = stream_seed(A.seed, it.stream);
+        p = it.draw0;
+        left = it.n;
+        valid = left > 0;
+    }
+    unsigned long long screened = 0;
+    unsigned int gk = 0;
+    uint32_t round = 0;
+
+    for (;;) {
+        __syncthreads();
+        const unsigned int bn = s_buf_n;  // nobody appends until after the next barrier
+        const int any = __syncthreads_or(valid);
+        if (bn > A.buf_cap - kRounds * kThreads || (!any && bn > 0)) {
+            cta_sort_desc(E, A.sort_n);
+            for (uint32_t i = A.kpad + tid; i < A.sort_n; i += kThreads) E[i] = Entry{0ull, 0ull};
+            if (tid == 0) {
+                s_buf_n = 0;
+                const Entry kth = E[A.keep - 1];
+                if (kth.k1 != 0ull) {
+                    s_t1 = kth.k1;
+                    s_t2 = kth.k2;
+                    const unsigned int ok = static_cast<unsigned int>(kth.k1 >> 32);
+                    s_ts = okey_score(ok);
+                    atomicMax(&A.ctrl->gtau, ok);
+                }
+            }
+            __syncthreads();
+        }
+        if (!any) break;
+        unsigned long long t1 = s_t1, t2 = s_t2;
+        float ts = s_ts;
+        if ((round++ & 7u) == 0) gk = *reinterpret_cast<volatile unsigned int *>(&A.ctrl->gtau);
+        if ((static_cast<unsigned long long>(gk) << 32) > t1) {
+            t1 = static_cast<unsigned long long>(gk) << 32;
+            t2 = 0;
+            ts = okey_score(gk);
+        }
+#pragma unroll 1
+        for (int r = 0; r < kRounds && valid; ++r) {
+            const CandHead h = cand_head(A.sc, seed_t, p);
+            const float s = synth_score<kFastDelta, false>(A.m, A.sc, el, seed_t, p, h, nullptr);
+            if (s >= ts) {
+                const unsigned long long k1 =
+                    (static_cast<unsigned long long>(score_okey(s)) << 32) | static_cast<unsigned int>(~item);
+                const unsigned long long k2 =
+                    (static_cast<unsigned long long>(~dcand) << 32) | ddraw;
+                if (k1 > t1 || (k1 == t1 && k2 > t2)) {
+                    const unsigned int slot = atomicAdd(&s_buf_n, 1u);
+                    buf[slot] = Entry{k1, k2};
+                }
+            }
+            p += h.len;
+            ddraw += h.len;
+            ++dcand;
+            ++screened;
+            if (--left == 0) {
+                item = atomicAdd(&A.ctrl->next_item, 1u);
+                valid = item < n_items;
+                if (valid) {
+                    const Item it = A.items[item];
+                    seed_t = stream_seed(A.seed, it.stream);
+                    p = it.draw0;
+                    left = it.n;
+                    dcand = 0;
+                    ddraw = 0;
+                    valid = left > 0;
+                }
+            }
+        }
+    }
+    // CTA list out (the last iteration merged any pending buffer)
+    Entry *out = A.lists + static_cast<size_t>(blockIdx.x) * A.kpad;
+    for (uint32_t i = tid; i < A.kpad; i += kThreads) out[i] = E[i];
+    // screened count: warp reduce then one atomic per warp
+    for (int o = 16; o > 0; o >>= 1) screened += __shfl_down_sync(0xffffffffu, screened, o);
+    if ((tid & 31) == 0) atomicAdd(&A.ctrl->screened, screened);
+}
+
+// ---- 5. merge tree ------------------------------------------------------------------
+
+__global__ void merge_kernel(const Entry *__restrict__ in, uint32_t nl, Entry *__restrict__ out,
+                             uint32_t kpad) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Entry *S = reinterpret_cast<Entry *>(smem_raw);
+    const uint32_t j = blockIdx.x, a = 2 * j, b = 2 * j + 1;
+    const Entry *la = in + static_cast<size_t>(a) * kpad;
+    Entry *o = out + static_cast<size_t>(j) * kpad;
+    if (b >= nl) {
+        for (uint32_t i = threadIdx.x; i < kpad; i += blockDim.x) o[i] = la[i];
+        return;
+    }
+    const Entry *lb = in + static_cast<size_t>(b) * kpad;
+    for (uint32_t i = threadIdx.x; i < kpad; i += blockDim.x) {
+        S[i] = la[i];
+        S[2 * kpad - 1 - i] = lb[i];  // descending ++ ascending: bitonic
+    }
+    __syncthreads();
+    for (uint32_t stride = kpad; stride > 0; stride >>= 1) {
+        for (uint32_t i = threadIdx.x; i < kpad; i += blockDim.x) {
+            const uint32_t lo = 2 * i - (i & (stride - 1));
+            const uint32_t hi = lo + stride;
+            const Entry x = S[lo], y = S[hi];
+            if (better(y, x)) {
+                S[lo] = y;
+                S[hi] = x;
+            }
+        }
+        __syncthreads();
+    }
+    for (uint32_t i = threadIdx.x; i < kpad; i += blockDim.x) o[i] = S[i];
+}
+
+// ---- 6. regenerate survivors ------------------------------------------------------
+
+template <bool kFastDelta>
+__global__ void regen_kernel(const __grid_constant__ ScreenArgs A, const Entry *__restrict__ fin,
+                             const unsigned long long *__restrict__ ids,
+                             const unsigned int *__restrict__ tribes, csx_survivor *__restrict__ out,
+                             unsigned long long *__restrict__ result) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= A.keep) return;
+    const Entry e = fin[q];
+    const bool real = e.k1 != 0ull;
+    const bool next_real = (q + 1 < A.keep) ? (fin[q + 1].k1 != 0ull) : false;
+    if (q == 0 && !real) A.ctrl->n_out = 0;
+    if (real && !next_real) A.ctrl->n_out = q + 1;
+    if (!real) return;
+    const uint32_t item = ~static_cast<uint32_t>(e.k1);
+    const uint32_t dcand = ~static_cast<uint32_t>(e.k2 >> 32);
+    const uint32_t ddraw = static_cast<uint32_t>(e.k2);
+    const Item it = A.items[item];
+    const uint64_t seed_t = stream_seed(A.seed, it.stream);
+    const uint64_t draw = it.draw0 + ddraw;
+    const CandHead h = cand_head(A.sc, seed_t, draw);
+    float genes[kNtot];
+    const float s = synth_score<kFastDelta, true>(A.m, A.sc, A.el, seed_t, draw, h, genes);
+    if (score_okey(s) != static_cast<unsigned int>(e.k1 >> 32)) atomicOr(&A.ctrl->err, kErrRegen);
+    csx_survivor v;
+    v.score = s;
+    v.tribe = tribes[h.ea];
+    v.pa = ids[h.ea];
+    v.pb = ids[h.eb];
+    v.stream = it.stream;
+    v.index = it.idx0 + dcand;
+    v.draw = draw;
+#pragma unroll
+    for (int k = 0; k < kNtot; ++k) v.g[k] = genes[k];
+    v.reserved = 0;
+    out[q] = v;
+}
+
+__global__ void result_kernel(const Ctrl *__restrict__ ctrl, unsigned long long *__restrict__ result) {
+    if (threadIdx.x == 0) {
+        result[0] = ctrl->n_out;
+        result[1] = ctrl->screened;
+        result[2] = ctrl->err;
+        result[3] = ctrl->n_items;
+    }
+}
+
+// ---- host orchestration ------------------------------------------------------------
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t n) {
+        if (n <= cap) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        const size_t want = std::max<size_t>(n, 256);
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+};
+
+struct Context {
+    std::mutex mu;
+    bool init = false;
+    int num_sms = 0;
+    size_t max_smem = 0;
+    cudaEvent_t done = nullptr;
+    cudaEvent_t ev[6] = {};
+    bool timed = false;
+    csx_run_info info{};
+    DevBuf genomes, tab, ids, tribes, recs, ck, segout, off, items, lists_a, lists_b, ctrl, surv,
+        result;
+};
+
+Context g_ctx[64];
+
+uint64_t env_u64(const char *name, uint64_t dflt) {
+    const char *v = std::getenv(name);
+    if (!v || !*v) return dflt;
+    char *end = nullptr;
+    const unsigned long long x = std::strtoull(v, &end, 10);
+    return (end && *end == 0 && x > 0) ? x : dflt;
+}
+
+uint32_t pow2_at_least(uint64_t x) {
+    uint32_t p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+// unit() < p  <=>  (next() >> 40) < thr  (unit is exact: k * 2^-24)
+uint32_t unit_threshold(float prob) {
+    if (!(prob > 0.0f)) return 0;  // also NaN: the comparison is always false
+    if (prob >= 1.0f) return 1u << 24;
+    const double x = std::ldexp(static_cast<double>(prob), 24);  // exact
+    return static_cast<uint32_t>(std::ceil(x));
+}
+
+#define CSX_CUDA(call)                                                                        \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess) {                                                              \
+            std::fprintf(stderr, "csx: %s failed: %s\n", #call, cudaGetErrorString(e_));     \
+            return e_ == cudaErrorMemoryAllocation ? CSX_ERR_OOM : CSX_ERR_CUDA;               \
+        }                                                                                     \
+    } while (0)
+
+struct Plan {
+    StreamGeom g;
+    bool short_path = false;
+    uint64_t items_cap = 0;
+    uint32_t kpad = 0, sort_n = 0, buf_cap = 0;
+    int grid = 0;
+    size_t smem = 0;
+    bool fast_delta = true;
+};
+
+int context_init(Context &cx, int dev) {
+    if (cx.init) return CSX_OK;
+    int v = 0;
+    CSX_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
+    cx.num_sms = v;
+    CSX_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    cx.max_smem = static_cast<size_t>(v);
+    CSX_CUDA(cudaEventCreateWithFlags(&cx.done, cudaEventDisableTiming));
+    for (auto &e : cx.ev) CSX_CUDA(cudaEventCreate(&e));
+    cx.init = true;
+    return CSX_OK;
+}
+
+template <bool kFast>
+int occupancy(const Context &cx, size_t smem, int *blocks) {
+    CSX_CUDA(cudaFuncSetAttribute(screen_kernel<kFast>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(smem)));
+    int nb = 0;
+    CSX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, screen_kernel<kFast>, kThreads, smem));
+    *blocks = std::max(1, nb) * cx.num_sms;
+    return CSX_OK;
+}
+
+int make_plan(const Context &cx, const csx_cfg &cfg, int ne, Plan *pl) {
+    StreamGeom &g = pl->g;
+    g.seed = cfg.seed;
+    g.T = std::max<uint64_t>(1, std::min<uint64_t>(cfg.threads, cfg.lambda));  // src/screen.zig:267
+    g.per = cfg.lambda / g.T;
+    g.my_last = cfg.lambda - (g.T - 1) * g.per;
+    const uint64_t my_max = std::max(g.per, g.my_last);
+    if (g.T >= 0xFFFFFFFFull) return CSX_ERR_LIMIT;
+    pl->fast_delta = std::isfinite(cfg.sigma) && std::fabs(cfg.sigma) <= 1.0e38f;
+
+    pl->kpad = std::max<uint32_t>(32, pow2_at_least(cfg.keep));
+    pl->sort_n = pow2_at_least(pl->kpad + 2ull * kRounds * kThreads);
+    pl->buf_cap = pl->sort_n - pl->kpad;
+    pl->smem = static_cast<size_t>(pl->sort_n) * sizeof(Entry) +
+               static_cast<size_t>(ne + 1) * kNtot * sizeof(float);
+    if (pl->smem + 1024 > cx.max_smem) return CSX_ERR_LIMIT;
+    int rc = pl->fast_delta ? occupancy<true>(cx, pl->smem, &pl->grid)
+                            : occupancy<false>(cx, pl->smem, &pl->grid);
+    if (rc) return rc;
+
+    // item size D: about eight items per screen thread
+    uint64_t d = env_u64("CSX_ITEM_CANDS", 0);
+    if (d == 0) {
+        const uint64_t target = 8ull * static_cast<uint64_t>(pl->grid) * kThreads;
+        d = std::max<uint64_t>(1, cfg.lambda / target);
+        d = std::min<uint64_t>(16384, std::max<uint64_t>(64, d));
+    }
+    uint32_t dl = 0;
+    while ((2ull << dl) <= d) ++dl;  // D = 2^dl <= d
+    g.d_log2 = dl;
+    const uint64_t D = 1ull << dl;
+
+    // candidate length is constant when neither branch probability is mixed
+    const uint32_t it = unit_threshold(cfg.imm_p), jt = unit_threshold(cfg.jump_p);
+    uint64_t gran = 2;
+    if ((it == 0 || it == (1u << 24)) && (jt == 0 || jt == (1u << 24)))
+        gran = (it ? 33 : 62) + (jt ? 2 : 0);
+    const uint64_t seg = env_u64("CSX_SEG_CANDS", kDefaultSegCands);
+    uint64_t L = 64 * std::min(seg, my_max);
+    L = ((L + gran - 1) / gran) * gran;
+    g.L = L;
+    g.C = static_cast<uint32_t>(std::max<uint64_t>(1, (64 * g.per + L - 1) / L));
+    g.C_last = static_cast<uint32_t>(std::max<uint64_t>(1, (64 * g.my_last + L - 1) / L));
+    g.n_seg = (g.T - 1) * g.C + g.C_last;
+    g.ckcap = static_cast<uint32_t>((2 * L / 33) / D + 3);
+    pl->short_path = my_max <= D;
+    pl->items_cap = pl->short_path ? g.T : g.n_seg * (static_cast<uint64_t>(g.ckcap) + 1);
+    if (pl->items_cap >= 0xFFFFFFFFull) return CSX_ERR_LIMIT;
+    return CSX_OK;
+}
+
+int unit_blocks(uint64_t n, int threads) { return static_cast<int>((n + threads - 1) / threads); }
+
+// Enqueue the whole pipeline on `st`. Device inputs: genomes (csx_genome x ne).
+int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, const csx_genome *d_genomes,
+                   int ne, csx_survivor *d_out, unsigned long long *d_result, cudaStream_t st) {
+    Plan pl;
+    int rc = make_plan(cx, cfg, ne, &pl);
+    if (rc) return rc;
+    const StreamGeom &g = pl.g;
+    const bool fast = pl.fast_delta;
+
+    CSX_CUDA(cx.tab.ensure(static_cast<size_t>(ne + 1) * kNtot * sizeof(float)));
+    CSX_CUDA(cx.ids.ensure(static_cast<size_t>(ne) * sizeof(unsigned long long)));
+    CSX_CUDA(cx.tribes.ensure(static_cast<size_t>(ne) * sizeof(unsigned int)));
+    CSX_CUDA(cx.ctrl.ensure(sizeof(Ctrl)));
+    CSX_CUDA(cx.items.ensure(pl.items_cap * sizeof(Item)));
+    const uint32_t nl = static_cast<uint32_t>(pl.grid);
+    CSX_CUDA(cx.lists_a.ensure(static_cast<size_t>(nl) * pl.kpad * sizeof(Entry)));
+    CSX_CUDA(cx.lists_b.ensure(static_cast<size_t>((nl + 1) / 2) * pl.kpad * sizeof(Entry)));
+    if (!pl.short_path) {
+        CSX_CUDA(cx.recs.ensure(g.n_seg * sizeof(SegRec)));
+        CSX_CUDA(cx.ck.ensure(g.n_seg * g.ckcap * sizeof(uint64_t)));
+        CSX_CUDA(cx.segout.ensure(g.n_seg * sizeof(SegOut)));
+        CSX_CUDA(cx.off.ensure(g.n_seg * sizeof(uint32_t)));
+    }
+    Ctrl *ctrl = static_cast<Ctrl *>(cx.ctrl.p);
+    CSX_CUDA(cudaStreamWaitEvent(st, cx.done, 0));
+    cx.timed = (cfg.flags & CSX_FLAG_STAGE_TIMES) != 0;
+    cx.info = csx_run_info{};
+    cx.info.screen_ctas = static_cast<uint32_t>(pl.grid);
+    cx.info.segments = pl.short_path ? 0 : g.n_seg;
+    cx.info.seg_draws = pl.short_path ? 0 : g.L;
+    cx.info.item_cands = 1ull << g.d_log2;
+    uint32_t launches = 0;
+    auto mark = [&](int i) -> cudaError_t { return cx.timed ? cudaEventRecord(cx.ev[i], st) : cudaSuccess; };
+    CSX_CUDA(mark(0));
+    CSX_CUDA(cudaMemsetAsync(ctrl, 0, sizeof(Ctrl), st));
+
+    SynthConst sc;
+    sc.ne = static_cast<uint32_t>(ne);
+    sc.ne_magic = ~0ull / static_cast<uint64_t>(ne) + 1;
+    sc.imm_thr = unit_threshold(cfg.imm_p);
+    sc.jump_thr = unit_threshold(cfg.jump_p);
+    sc.sigma = cfg.sigma;
+    sc.nsig1 = -cfg.sigma;
+    sc.nsig2 = -2.0f * cfg.sigma;
+
+    float *tab = static_cast<float *>(cx.tab.p);
+    auto *ids = static_cast<unsigned long long *>(cx.ids.p);
+    auto *tribes = static_cast<unsigned int *>(cx.tribes.p);
+    prep_elites_kernel<<<unit_blocks(static_cast<uint64_t>(ne + 1) * kNtot, 256), 256, 0, st>>>(
+        d_genomes, ne, tab, ids, tribes);
+    CSX_CUDA(cudaGetLastError());
+    ++launches;
+    CSX_CUDA(mark(1));
+
+    Item *items = static_cast<Item *>(cx.items.p);
+    if (pl.short_path) {
+        stream_items_kernel<<<unit_blocks(g.T, 256), 256, 0, st>>>(g, items, ctrl);
+        CSX_CUDA(cudaGetLastError());
+        ++launches;
+    } else {
+        auto *recs = static_cast<SegRec *>(cx.recs.p);
+        auto *ck = static_cast<uint64_t *>(cx.ck.p);
+        auto *so = static_cast<SegOut *>(cx.segout.p);
+        auto *off = static_cast<uint32_t *>(cx.off.p);
+        walk_kernel<<<unit_blocks(g.n_seg, 128), 128, 0, st>>>(sc, g, recs, ck, ctrl);
+        CSX_CUDA(cudaGetLastError());
+        assemble_kernel<<<unit_blocks(g.T, 128), 128, 0, st>>>(g, recs, so, ctrl);
+        CSX_CUDA(cudaGetLastError());
+        scan_kernel<<<1, 1024, 0, st>>>(so, g.n_seg, off, ctrl, pl.items_cap);
+        CSX_CUDA(cudaGetLastError());
+        emit_kernel<<<unit_blocks(g.n_seg, 128), 128, 0, st>>>(g, so, off, ck, items, ctrl);
+        CSX_CUDA(cudaGetLastError());
+        launches += 4;
+    }
+    CSX_CUDA(mark(2));
+
+    ScreenArgs A;
+    A.m.w0 = model.w0;
+    for (int k = 0; k < kNtot; ++k) A.m.wlin[k] = model.w_lin[k];
+    for (int i = 0; i < 16; ++i)
+        for (int j = 0; j <= i; ++j) A.m.wq[tri(i, j)] = model.w_quad[i * 16 + j];
+    A.sc = sc;
+    A.seed = cfg.seed;
+    A.el = tab;
+    A.items = items;
+    A.ctrl = ctrl;
+    A.lists = static_cast<Entry *>(cx.lists_a.p);
+    A.keep = static_cast<uint32_t>(cfg.keep);
+    A.kpad = pl.kpad;
+    A.sort_n = pl.sort_n;
+    A.buf_cap = pl.buf_cap;
+    if (fast)
+        screen_kernel<true><<<pl.grid, kThreads, pl.smem, st>>>(A);
+    else
+        screen_kernel<false><<<pl.grid, kThreads, pl.smem, st>>>(A);
+    CSX_CUDA(cudaGetLastError());
+    ++launches;
+    CSX_CUDA(mark(3));
+
+    // merge tree
+    const size_t msmem = 2ull * pl.kpad * sizeof(Entry);
+    CSX_CUDA(cudaFuncSetAttribute(merge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(msmem)));
+    Entry *cur = static_cast<Entry *>(cx.lists_a.p), *nxt = static_cast<Entry *>(cx.lists_b.p);
+    uint32_t n = nl;
+    while (n > 1) {
+        const uint32_t m = (n + 1) / 2;
+        merge_kernel<<<m, 256, msmem, st>>>(cur, n, nxt, pl.kpad);
+        CSX_CUDA(cudaGetLastError());
+        ++launches;
+        std::swap(cur, nxt);
+        n = m;
+    }
+    CSX_CUDA(mark(4));
+    if (fast)
+        regen_kernel<true><<<unit_blocks(cfg.keep, 128), 128, 0, st>>>(A, cur, ids, tribes, d_out, d_result);
+    else
+        regen_kernel<false><<<unit_blocks(cfg.keep, 128), 128, 0, st>>>(A, cur, ids, tribes, d_out, d_result);
+    CSX_CUDA(cudaGetLastError());
+    result_kernel<<<1, 32, 0, st>>>(ctrl, d_result);
+    CSX_CUDA(cudaGetLastError());
+    launches += 2;
+    CSX_CUDA(mark(5));
+    cx.info.launches = launches;
+    CSX_CUDA(cudaEventRecord(cx.done, st));
+    return CSX_OK;
+}
+
+int check_common(const csx_cfg *cfg, const csx_model *model, int ne) {
+    if (!cfg || !model) return CSX_ERR_BAD_ARGS;
+    if (ne < 2) return CSX_ERR_NEED_TWO_ELITES;  // src/screen.zig:266
+    if (cfg->keep == 0) return CSX_ERR_BAD_ARGS;  // Heap.offer would read slots[0] of an empty heap
+    if (cfg->keep > kMaxKeep || static_cast<uint32_t>(ne) > kMaxElites) return CSX_ERR_LIMIT;
+    return CSX_OK;
+}
+
+int current_context(Context **out) {
+    int dev = 0;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return CSX_ERR_NO_DEVICE;
+    }
+    CSX_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return CSX_ERR_LIMIT;
+    *out = &g_ctx[dev];
+    return CSX_OK;
+}
+
+}  // namespace csx
+
+using namespace csx;
+
+extern "C" {
+
+int csx_last_run_info(csx_run_info *out) {
+    if (!out) return CSX_ERR_BAD_ARGS;
+    Context *cx = nullptr;
+    int rc = current_context(&cx);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lock(cx->mu);
+    *out = cx->info;
+    if (cx->init && cx->timed) {
+        CSX_CUDA(cudaEventSynchronize(cx->ev[5]));
+        float *ms[5] = {&out->ms_prep, &out->ms_items, &out->ms_screen, &out->ms_merge, &out->ms_regen};
+        for (int i = 0; i < 5; ++i) CSX_CUDA(cudaEventElapsedTime(ms[i], cx->ev[i], cx->ev[i + 1]));
+        CSX_CUDA(cudaEventElapsedTime(&out->ms_total, cx->ev[0], cx->ev[5]));
+    }
+    return CSX_OK;
+}
+
+int csx_limits(uint64_t *max_keep, uint64_t *max_elites) {
+    if (max_keep) *max_keep = kMaxKeep;
+    if (max_elites) *max_elites = kMaxElites;
+    return CSX_OK;
+}
+
+int csx_screen_device(const csx_cfg *cfg, const csx_model *model, const csx_genome *d_elites, int n_elites,
+                      csx_survivor *d_out, uint64_t out_cap, uint64_t *d_result, void *cuda_stream) {
+    int rc = check_common(cfg, model, n_elites);
+    if (rc) return rc;
+    if (!d_elites || !d_result || (!d_out && cfg->lambda > 0)) return CSX_ERR_BAD_ARGS;
+    if (out_cap < std::min<uint64_t>(cfg->keep, cfg->lambda)) return CSX_ERR_BAD_ARGS;
+    Context *cx = nullptr;
+    rc = current_context(&cx);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lock(cx->mu);
+    int dev = 0;
+    CSX_CUDA(cudaGetDevice(&dev));
+    rc = context_init(*cx, dev);
+    if (rc) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+    if (cfg->lambda == 0) {  // one empty stream: nothing screened, nothing kept
+        CSX_CUDA(cudaStreamWaitEvent(st, cx->done, 0));
+        CSX_CUDA(cudaMemsetAsync(d_result, 0, 4 * sizeof(uint64_t), st));
+        CSX_CUDA(cudaEventRecord(cx->done, st));
+        return CSX_OK;
+    }
+    csx_cfg c = *cfg;
+    return enqueue_screen(*cx, c, *model, d_elites, n_elites, d_out,
+                          reinterpret_cast<unsigned long long *>(d_result), st);
+}
+
+int csx_screen(const csx_cfg *cfg, const csx_model *model, const csx_genome *elites, int n_elites,
+               csx_survivor *out, uint64_t out_cap, uint64_t *n_out, uint64_t *screened) {
+    if (n_out) *n_out = 0;
+    if (screened) *screened = 0;
+    int rc = check_common(cfg, model, n_elites);
+    if (rc) return rc;
+    if (!elites || !n_out || (!out && out_cap > 0)) return CSX_ERR_BAD_ARGS;
+    if (cfg->lambda == 0) return CSX_OK;
+    Context *cx = nullptr;
+    rc = current_context(&cx);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lock(cx->mu);
+    int dev = 0;
+    CSX_CUDA(cudaGetDevice(&dev));
+    rc = context_init(*cx, dev);
+    if (rc) return rc;
+    const uint64_t keep_n = std::min<uint64_t>(cfg->keep, cfg->lambda);
+    if (out_cap < keep_n && !(cfg->flags & CSX_FLAG_AS_SHIPPED)) return CSX_ERR_BAD_ARGS;
+    CSX_CUDA(cx->genomes.ensure(static_cast<size_t>(n_elites) * sizeof(csx_genome)));
+    CSX_CUDA(cx->surv.ensure(static_cast<size_t>(cfg->keep) * sizeof(csx_survivor)));
+    CSX_CUDA(cx->result.ensure(4 * sizeof(uint64_t)));
+    cudaStream_t st = nullptr;
+    CSX_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    auto *dg = static_cast<csx_genome *>(cx->genomes.p);
+    auto *ds = static_cast<csx_survivor *>(cx->surv.p);
+    auto *dr = static_cast<unsigned long long *>(cx->result.p);
+    unsigned long long res[4] = {0, 0, 0, 0};
+    cudaError_t e = cudaMemcpyAsync(dg, elites, static_cast<size_t>(n_elites) * sizeof(csx_genome),
+                                    cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+        rc = enqueue_screen(*cx, *cfg, *model, dg, n_elites, ds, dr, st);
+        if (rc == CSX_OK) {
+            e = cudaMemcpyAsync(res, dr, sizeof(res), cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            const uint64_t cnt = std::min<uint64_t>(res[0], keep_n);
+            if (e == cudaSuccess && res[2] == 0 && cnt > 0 && !(cfg->flags & CSX_FLAG_AS_SHIPPED)) {
+                e = cudaMemcpyAsync(out, ds, cnt * sizeof(csx_survivor), cudaMemcpyDeviceToHost, st);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            }
+        }
+    }
+    cudaStreamDestroy(st);
+    if (e != cudaSuccess) {
+        std::fprintf(stderr, "csx: %s\n", cudaGetErrorString(e));
+        return CSX_ERR_CUDA;
+    }
+    if (rc) return rc;
+    if (res[2] != 0) {
+        std::fprintf(stderr, "csx: device error flags 0x%llx\n", res[2]);
+        return CSX_ERR_DEVICE_STATE;
+    }
+    cx->info.items = res[3];
+    *n_out = (cfg->flags & CSX_FLAG_AS_SHIPPED) ? 0 : std::min<uint64_t>(res[0], keep_n);
+    if (screened) *screened = res[1];
+    return CSX_OK;
+}
+
+}  // extern "C"

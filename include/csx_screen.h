@@ -1,0 +1,179 @@
+/*
+ * csx_screen.h — C ABI of the GB300 screen funnel (libcsx_screen.so).
+ *
+ * The reference exposes its screen as a process boundary: the `arena screen`
+ * verb (src/main.zig:98-101,156-218) reads a surrogate file and an elites
+ * file, runs src/screen.zig:run and writes the promoted survivors and the
+ * candidate count. This header is the in-process replacement for that
+ * boundary: plain pointers and sizes, integer status codes, no exceptions and
+ * no C++ or torch types. Every entry point names the reference symbol it
+ * replaces.
+ *
+ * Threading: every call is synchronous unless it takes a `cuda_stream`
+ * argument. Calls may come from several host threads; device scratch is kept
+ * per device and guarded by a lock.
+ */
+#ifndef CSX_SCREEN_H
+#define CSX_SCREEN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CSX_ABI_VERSION 1
+
+#define CSX_NG 23   /* effector genes   (src/genome.zig:14) */
+#define CSX_NR 6    /* regulator genes  (src/genome.zig:15) */
+#define CSX_NTOT 29 /* flat genome size (src/genome.zig:16) */
+
+/* Status codes. The first three mirror the Zig errors of the screen path. */
+enum {
+    CSX_OK = 0,
+    CSX_ERR_BAD_MODEL = -1,       /* error.BadModel       src/screen.zig:37,120 */
+    CSX_ERR_NEED_TWO_ELITES = -2, /* error.NeedTwoElites  src/screen.zig:266, src/main.zig:214 */
+    CSX_ERR_BAD_ARGS = -3,        /* error.BadArgs        src/main.zig:166 */
+    CSX_ERR_PARSE = -4,           /* std.fmt.parseInt / parseFloat failure */
+    CSX_ERR_IO = -5,              /* file open / read / write failure */
+    CSX_ERR_LIMIT = -6,           /* size beyond this build's device limits */
+    CSX_ERR_CUDA = -7,            /* a CUDA runtime call failed */
+    CSX_ERR_NO_DEVICE = -8,       /* no CUDA device visible */
+    CSX_ERR_OOM = -9,             /* host or device allocation failed */
+    CSX_ERR_DEVICE_STATE = -10    /* a kernel raised its error flag */
+};
+
+/* Flags for csx_cfg.flags and the parse / format calls. */
+#define CSX_FLAG_AS_SHIPPED 0x1u   /* write no survivors, as the shipped binary does
+                                      (src/screen.zig:221,285,309-313) */
+#define CSX_FLAG_OUTPUT_29 0x2u    /* survivor lines in the reference's 29-token form
+                                      (src/screen.zig:327-336); default is the 34-token
+                                      v6 pop line (src/genome.zig:191-201) */
+#define CSX_FLAG_PARSE_V6_FIX 0x4u /* 34-token elite lines keep genes 16..21; as written
+                                      the reference sets them to 0.0 (src/genome.zig:138-158) */
+#define CSX_FLAG_EXACT_ALL 0x8u    /* score every candidate in the reference's f32 order
+                                      instead of filtering with a certified fast score */
+#define CSX_FLAG_STAGE_TIMES 0x10u /* record per-stage device times (csx_last_run_info) */
+
+/* Model: the flat weight layout of src/screen.zig:23-27. */
+typedef struct csx_model {
+    float w0;
+    float w_lin[CSX_NTOT];
+    float w_quad[256]; /* 16x16 over the legacy effectors, zero strict upper triangle */
+} csx_model;
+
+/* Genome: src/genome.zig:78-86, genes flattened to 23 effectors + 6 regulators
+ * (the order src/screen.zig:240-241 reads them in). */
+typedef struct csx_genome {
+    uint64_t id;
+    uint64_t pa;
+    uint64_t pb;
+    uint32_t gen;
+    uint32_t tribe;
+    float g[CSX_NTOT];
+    uint32_t reserved;
+} csx_genome;
+
+/* Screen configuration: src/screen.zig:129-137 (Cfg). */
+typedef struct csx_cfg {
+    uint64_t lambda;  /* candidates to synthesise (the --lambda count) */
+    uint64_t keep;    /* survivors to keep (K) */
+    uint64_t seed;    /* base seed; stream t uses seed ^ (0x9E3779B97F4A7C15 * (t+1)) */
+    uint64_t threads; /* RNG stream count T, part of the result's identity */
+    float sigma;      /* mutation half-width */
+    float jump_p;     /* jump probability */
+    float imm_p;      /* immigrant probability */
+    uint32_t flags;   /* CSX_FLAG_* */
+} csx_cfg;
+
+/* Survivor: the Slot of src/screen.zig:145-149 plus its provenance. */
+typedef struct csx_survivor {
+    float score;      /* Model.score in the reference's f32 op order */
+    uint32_t tribe;   /* lineage tribe: the first parent's tribe */
+    uint64_t pa;      /* lineage: first parent's id */
+    uint64_t pb;      /* lineage: second parent's id */
+    uint64_t stream;  /* RNG stream t */
+    uint64_t index;   /* candidate index within stream t */
+    uint64_t draw;    /* splitmix64 draw position of the candidate's first draw */
+    float g[CSX_NTOT];
+    uint32_t reserved;
+} csx_survivor;
+
+/* ---- library ---------------------------------------------------------- */
+
+int csx_abi_version(void);
+const char *csx_strerror(int status);
+/* Defaults of src/screen.zig:129-137 and src/main.zig:161. */
+void csx_cfg_default(csx_cfg *cfg);
+
+/* ---- model and genome I/O (host) --------------------------------------- */
+
+/* Model.fromCompact, src/screen.zig:36-95: n in {153,159,161,164,165,166}. */
+int csx_model_from_compact(const float *w, int n, csx_model *out);
+/* loadModel's text body, src/screen.zig:115-127: "n w0 w1 ...". */
+int csx_model_parse(const char *text, size_t len, float *w, int cap, int *n_out);
+/* parseLine, src/genome.zig:116-188. Returns 1 (parsed), 0 (not a genome
+ * line: wrong token count or comment) or a negative status. */
+int csx_genome_parse_line(const char *line, size_t len, uint32_t flags, csx_genome *out);
+/* The elites loop of src/main.zig:201-214: skips blank, '#' and bad lines.
+ * *n_out is the number of genomes found (may exceed cap; only cap stored). */
+int csx_elites_parse(const char *text, size_t len, uint32_t flags, csx_genome *out, int cap,
+                     int *n_out);
+/* formatLine, src/genome.zig:191-201 (34 tokens). Returns chars written. */
+int csx_genome_format_line(const csx_genome *g, char *buf, size_t cap);
+/* One promoted line: src/screen.zig:327-336 with CSX_FLAG_OUTPUT_29, else the
+ * 34-token v6 form with id and gen 0. Returns chars written (with '\n'). */
+int csx_survivor_format_line(const csx_survivor *s, uint32_t flags, char *buf, size_t cap);
+
+/* ---- the screen (GPU) --------------------------------------------------- */
+
+/* run(), src/screen.zig:257-343, without the file output: host buffers in and
+ * out. Writes min(keep, lambda) survivors (0 with CSX_FLAG_AS_SHIPPED) sorted
+ * by score descending, ties by (stream, index) ascending; *screened is the
+ * candidate count the reference writes to --count-out. Synchronous. */
+int csx_screen(const csx_cfg *cfg, const csx_model *model, const csx_genome *elites,
+               int n_elites, csx_survivor *out, uint64_t out_cap, uint64_t *n_out,
+               uint64_t *screened);
+
+/* Same, with device-resident elites and survivors, enqueued on `cuda_stream`
+ * (a cudaStream_t; NULL = the legacy default stream). d_result receives four
+ * device uint64: survivor count, screened count, device error bits (0 = ok)
+ * and a reserved word. The call returns after enqueueing; calls on different
+ * streams are ordered after one another by the library. */
+int csx_screen_device(const csx_cfg *cfg, const csx_model *model, const csx_genome *d_elites,
+                      int n_elites, csx_survivor *d_out, uint64_t out_cap, uint64_t *d_result,
+                      void *cuda_stream);
+
+/* The `arena screen` verb, src/main.zig:156-218 plus run()'s file output
+ * (src/screen.zig:321-342): argv holds the flags after "screen". Returns 0
+ * or a negative status; a message is printed to stderr on failure. */
+int csx_screen_cli(int argc, const char *const *argv);
+
+/* Device limits of this build (for callers that want to check first). */
+int csx_limits(uint64_t *max_keep, uint64_t *max_elites);
+
+/* Shape and stage times of the last screen enqueued on the current device.
+ * No reference counterpart: the reference only prints the candidate count
+ * (src/main.zig:217). Stage times need CSX_FLAG_STAGE_TIMES and wait for the
+ * last call to finish. */
+typedef struct csx_run_info {
+    uint32_t launches;      /* kernels the call enqueued */
+    uint32_t screen_ctas;   /* persistent screen CTAs */
+    uint64_t segments;      /* walk segments (0 when streams fit one item) */
+    uint64_t seg_draws;     /* draws per walk segment */
+    uint64_t item_cands;    /* candidates per work item (D) */
+    uint64_t items;         /* work items the screen consumed */
+    float ms_prep;          /* elite table */
+    float ms_items;         /* walk, assemble, scan, emit */
+    float ms_screen;        /* the persistent screen kernel */
+    float ms_merge;         /* top-K merge tree */
+    float ms_regen;         /* survivor regeneration */
+    float ms_total;
+} csx_run_info;
+int csx_last_run_info(csx_run_info *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CSX_SCREEN_H */

@@ -1,0 +1,257 @@
+"""GPU screen vs the CPU oracle, through the C ABI (bit-exact).
+
+Survivors are compared field by field: score and gene bit patterns, lineage,
+stream, stream-local index and draw position. Sizes are ones the oracle
+finishes in seconds; the full-size generation is checked through properties
+(count, order, per-survivor regeneration by the oracle).
+"""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu(csx):
+    from conftest import has_gpu
+
+    if not has_gpu():
+        pytest.skip("no CUDA device")
+
+
+def _models():
+    from codec_arena_gb300 import workloads as wl
+
+    rng = np.random.default_rng(66)
+    return {
+        "v1_normal": wl.seeded_normal_model(seed=2),
+        "v3_committed": wl.surrogate_161(),
+        "v6_random": rng.normal(0, 3, 166).astype(np.float32),
+    }
+
+
+def _gpu(lam, keep, seed, T, w, el, sigma=0.12, jump=0.02, imm=0.01, flags=0):
+    from codec_arena_gb300 import screen
+
+    cfg = screen.Cfg(lam, keep, seed, threads=T, sigma=sigma, jump_p=jump, imm_p=imm, flags=flags)
+    return screen.screen(cfg, screen.Model.from_compact(w), el)
+
+
+def _orc(orc, lam, keep, seed, T, w, el, sigma=0.12, jump=0.02, imm=0.01, flags=0):
+    c = orc.cfg(lam, keep, seed, threads=T, sigma=sigma, jump_p=jump, imm_p=imm, flags=flags)
+    return orc.screen(c, orc.model_from_compact(w), el, cpu_threads=os.cpu_count() or 4)
+
+
+def assert_same(got, want):
+    assert len(got) == len(want), (len(got), len(want))
+    np.testing.assert_array_equal(got["score"].view(np.uint32), want["score"].view(np.uint32))
+    for f in ("stream", "index", "draw", "pa", "pb", "tribe"):
+        np.testing.assert_array_equal(got[f], want[f], err_msg=f)
+    np.testing.assert_array_equal(got["g"].view(np.uint32), want["g"].view(np.uint32))
+
+
+def check(orc, *args, **kw):
+    got, sg = _gpu(*args, **kw)
+    want, sw = _orc(orc, *args, **kw)
+    assert sg == sw
+    assert_same(got, want)
+    return got
+
+
+@pytest.fixture
+def env(monkeypatch):
+    return monkeypatch
+
+
+def test_basic_t4(orc):
+    from codec_arena_gb300 import workloads as wl
+
+    check(orc, 100_000, 32, 7, 4, wl.seeded_normal_model(), wl.seeded_elites(64))
+
+
+@pytest.mark.parametrize("name", ["v1_normal", "v3_committed", "v6_random"])
+def test_models(orc, name):
+    from codec_arena_gb300 import workloads as wl
+
+    check(orc, 60_000, 192, 3, 4, _models()[name], wl.seeded_elites(64))
+
+
+@pytest.mark.parametrize("T", [1, 2, 3, 7, 64, 999, 5000, 20000])
+def test_stream_counts(orc, T):
+    from codec_arena_gb300 import workloads as wl
+
+    check(orc, 20_000, 50, 11, T, wl.surrogate_161(), wl.seeded_elites(32))
+
+
+def test_one_candidate_per_stream(orc):
+    from codec_arena_gb300 import workloads as wl
+
+    check(orc, 3000, 40, 5, 3000, wl.surrogate_161(), wl.seeded_elites(16))
+    check(orc, 3000, 40, 5, 10**9, wl.surrogate_161(), wl.seeded_elites(16))
+
+
+@pytest.mark.parametrize("seg,item", [(500, 64), (37, 64), (3, 64), (1, 64), (2000, 4096)])
+def test_segment_linking(orc, env, seg, item):
+    """Short segments force the walk's meeting-point logic, including chains
+    that meet only several segments later."""
+    from codec_arena_gb300 import workloads as wl
+
+    env.setenv("CSX_SEG_CANDS", str(seg))
+    env.setenv("CSX_ITEM_CANDS", str(item))
+    check(orc, 40_000, 64, 9, 4, wl.surrogate_161(), wl.seeded_elites(64))
+    check(orc, 7_001, 20, 1, 3, wl.seeded_normal_model(), wl.seeded_elites(5), imm=0.3, jump=0.4)
+
+
+@pytest.mark.parametrize("imm,jump", [(0.0, 0.0), (1.0, 0.0), (1.0, 1.0), (0.0, 1.0), (0.0, 0.02),
+                                      (0.5, 0.5), (0.01, 0.0), (1e-7, 0.02), (float("nan"), 2.0)])
+def test_branch_probabilities(orc, env, imm, jump):
+    from codec_arena_gb300 import workloads as wl
+
+    env.setenv("CSX_SEG_CANDS", "300")
+    check(orc, 30_000, 40, 21, 4, wl.surrogate_161(), wl.seeded_elites(64), imm=imm, jump=jump)
+
+
+@pytest.mark.parametrize("sigma", [0.0, 0.5, 1e-30, 2.0, 3e38, float("inf"), -0.25])
+def test_sigma(orc, sigma):
+    from codec_arena_gb300 import workloads as wl
+
+    check(orc, 20_000, 30, 4, 4, wl.surrogate_161(), wl.seeded_elites(64), sigma=sigma)
+
+
+@pytest.mark.parametrize("keep", [1, 2, 31, 192, 1000, 4096])
+def test_keep(orc, keep):
+    from codec_arena_gb300 import workloads as wl
+
+    check(orc, 50_000, keep, 8, 4, wl.seeded_normal_model(), wl.seeded_elites(64))
+
+
+@pytest.mark.parametrize("ne", [2, 3, 17, 256, 1536])
+def test_elite_counts(orc, ne):
+    from codec_arena_gb300 import workloads as wl
+
+    check(orc, 30_000, 64, 12, 4, wl.surrogate_161(), wl.seeded_elites(ne, seed=ne))
+
+
+def test_small_lambda(orc):
+    from codec_arena_gb300 import workloads as wl
+
+    el = wl.seeded_elites(8)
+    w = wl.surrogate_161()
+    got = check(orc, 5, 100, 1, 4, w, el)      # fewer candidates than keep
+    assert len(got) == 5
+    got = check(orc, 1, 3, 1, 4, w, el)
+    assert len(got) == 1
+    got, s = _gpu(0, 10, 1, 4, w, el)
+    assert len(got) == 0 and s == 0
+
+
+def test_all_ties(orc):
+    """Zero surface: every score is 0. Ties go to (stream, index); the
+    reference's heaps keep each stream's first K and its stable sort keeps
+    stream order, which is the same list."""
+    from codec_arena_gb300 import workloads as wl
+
+    got = check(orc, 40_000, 100, 3, 4, np.zeros(153, np.float32), wl.seeded_elites(8))
+    assert list(got["index"]) == list(range(100))
+
+
+def test_elites_with_extreme_genes(orc):
+    from codec_arena_gb300 import genome, workloads as wl
+
+    el = wl.seeded_elites(12)
+    el["g"][0, :5] = [-0.0, -3.0, 7.5, np.inf, -np.inf]
+    el["g"][1, :3] = [np.nan, 1.0, 0.0]
+    check(orc, 20_000, 50, 2, 4, wl.surrogate_161(), el)
+
+
+def test_as_shipped(orc):
+    from codec_arena_gb300 import _lib, workloads as wl
+
+    got, s = _gpu(10_000, 10, 1, 4, wl.surrogate_161(), wl.seeded_elites(8), flags=_lib.FLAG_AS_SHIPPED)
+    assert len(got) == 0 and s == 10_000
+
+
+def test_repeatable_and_buffer_regrowth(orc):
+    from codec_arena_gb300 import workloads as wl
+
+    el = wl.seeded_elites(64)
+    w = wl.surrogate_161()
+    a, _ = _gpu(200_000, 256, 5, 4, w, el)
+    _gpu(1000, 4000, 5, 2, w, el)
+    _gpu(100, 3, 5, 100, w, wl.seeded_elites(1500))
+    b, _ = _gpu(200_000, 256, 5, 4, w, el)
+    assert a.tobytes() == b.tobytes()
+
+
+def test_prefix_1e8_t4(orc):
+    """The 1e8-candidate prefix of the full generation, T = 4 (the reference
+    CI's stream count), committed surrogate, 64 seeded elites, top 256."""
+    from codec_arena_gb300 import workloads as wl
+
+    check(orc, 100_000_000, 256, 7, 4, wl.surrogate_161(), wl.seeded_elites(64))
+
+
+def test_full_generation_properties(orc):
+    """2.65e9 candidates, T = 2^20 streams (short streams, so the oracle can
+    re-walk each survivor's stream): count, order, and every survivor
+    regenerated by the oracle from (stream, draw) with its index re-walked."""
+    from codec_arena_gb300 import workloads as wl
+
+    el = wl.seeded_elites(64)
+    w = wl.surrogate_161()
+    lam, T = 2_650_000_000, 1 << 20
+    got, screened = _gpu(lam, 256, 7, T, w, el)
+    assert screened == lam and len(got) == 256
+    s = got["score"].astype(np.float64)
+    assert np.all(s[:-1] >= s[1:])
+    c = orc.cfg(lam, 256, 7, threads=T)
+    m = orc.model_from_compact(w)
+    for r in got:
+        o, _ = orc.candidate(c, m, el, int(r["stream"]), int(r["draw"]))
+        assert o["score"].view(np.uint32) == r["score"].view(np.uint32)
+        assert o["g"].tobytes() == r["g"].tobytes()
+        assert (o["pa"], o["pb"], o["tribe"]) == (r["pa"], r["pb"], r["tribe"])
+        n, nxt = orc.walk(c, int(r["stream"]), 0, int(r["draw"]))
+        assert n == r["index"] and nxt == r["draw"]
+
+
+def test_cli_end_to_end(orc, tmp_path):
+    from codec_arena_gb300 import cli, genome, screen, workloads as wl
+
+    seed_pop = os.path.join(wl.GOLDEN_DIR, "pop_seed_96.txt")
+    for extra, flags, fix in (([], 0, False), (["--compat-29"], 2, False), (["--parse-v6-fix"], 0, True)):
+        out, cnt = tmp_path / "p.txt", tmp_path / "c.txt"
+        rc = cli.main(["screen", "--model", wl.SURROGATE_161, "--elites", seed_pop, "--out", str(out),
+                       "--count-out", str(cnt), "--lambda", "300000", "--keep", "192", "--seed", "7",
+                       "--threads", "4", *extra])
+        assert rc == 0
+        assert cnt.read_text() == "300000\n"
+        el = genome.load_elites(seed_pop, v6_fix=fix)
+        want, _ = _orc(orc, 300_000, 192, 7, 4, wl.surrogate_161(), el)
+        lines = out.read_text().splitlines(keepends=True)
+        assert len(lines) == 192
+        assert lines == [screen.format_survivor(r, flags) for r in want]
+
+
+def test_screen_device_torch_stream(orc):
+    import torch
+
+    from codec_arena_gb300 import _lib, screen, workloads as wl
+
+    el = wl.seeded_elites(64)
+    w = wl.surrogate_161()
+    cfg = screen.Cfg(150_000, 100, 4, threads=4)
+    d_el = torch.from_numpy(el.view(np.uint8).copy()).cuda()
+    d_out = torch.zeros(100 * _lib.SURVIVOR_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    d_res = torch.zeros(4, dtype=torch.int64, device="cuda")
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        screen.screen_device(cfg, screen.Model.from_compact(w), d_el, d_out, d_res)
+    s.synchronize()
+    res = d_res.cpu().numpy()
+    assert res[2] == 0 and res[1] == 150_000
+    got = screen.survivors_from_bytes(d_out.cpu().numpy(), int(res[0]))
+    want, _ = _orc(orc, 150_000, 100, 4, 4, w, el)
+    assert_same(got, want)
