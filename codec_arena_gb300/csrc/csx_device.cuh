@@ -119,7 +119,8 @@ __device__ __forceinline__ CandHead cand_head(const SynthConst &C, uint64_t seed
 //
 // kFastDelta: delta = fma(y, B, -c*B) with y in [1,2), c in {1,2}; -c*B is
 // exact, so this is one rounding of (y-c)*B == round((u-0.5)*2*B). Valid for
-// finite |B| <= 2^126; otherwise the two-op form is used.
+// finite |B| <= 1e38 (then |delta| < |B| is finite too); otherwise the
+// two-op form is used.
 template <bool kFastDelta, bool kKeepGenes>
 __device__ __forceinline__ float synth_score(const DevModel &M, const SynthConst &C,
                                              const float *__restrict__ el, uint64_t seed_t,
@@ -153,7 +154,12 @@ __device__ __forceinline__ float synth_score(const DevModel &M, const SynthConst
             const float nc = (static_cast<int32_t>(vh) < 0) ? -1.0f : -2.0f;
             g = __fadd_rn(par, __fmul_rn(__fadd_rn(y, nc), B));
         }
-        g = fmaxf(fminf(g, 1.0f), 0.0f);  // clamp01: NaN -> 1 as minnum
+        // clamp01 (NaN -> 1, as @min(1, NaN) == 1). The fast form's delta is
+        // finite and the elite table holds no NaN, so g is never NaN there.
+        if (kFastDelta)
+            g = fmaxf(fminf(g, 1.0f), 0.0f);
+        else
+            g = (g != g) ? 1.0f : fmaxf(fminf(g, 1.0f), 0.0f);
         g = (static_cast<uint32_t>(k) == h.jidx) ? h.jval : g;
         if (kKeepGenes) genes[k] = g;
         if (k < 16) {

@@ -120,14 +120,18 @@ __device__ __forceinline__ void split_range(uint64_t lo, uint64_t cnt, uint32_t 
 
 // ---- 0. elite table ---------------------------------------------------------
 
-// (ne + 1) x 29 table, row ne = 0.5 (the immigrant row); -0.0 genes become
-// +0.0 (clamp01 of a crossover gene can then never see -0.0).
+// (ne + 1) x 29 table, row ne = 0.5 (the immigrant row). -0.0 genes become
+// +0.0, so clamp01 of a crossover gene never sees -0.0; NaN genes become +inf:
+// the reference's clamp01(NaN + d) is 1 (@min returns the non-NaN operand),
+// and so is clamp01(inf + d) for the finite d of the fast delta form, whose
+// clamp the compiler may emit as a saturating add that flushes NaN to 0.
 __global__ void prep_elites_kernel(const csx_genome *__restrict__ el, int ne, float *__restrict__ tab,
                                    unsigned long long *__restrict__ ids, unsigned int *__restrict__ tribes) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < ne * kNtot) {
         const int r = i / kNtot, k = i - r * kNtot;
-        tab[i] = __fadd_rn(el[r].g[k], 0.0f);
+        const float v = el[r].g[k];
+        tab[i] = (v != v) ? INFINITY : __fadd_rn(v, 0.0f);
     } else if (i < (ne + 1) * kNtot) {
         tab[i] = 0.5f;
     }
