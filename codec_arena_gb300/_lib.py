@@ -103,6 +103,9 @@ SIGNATURES = {
     "csx_screen_device": (ctypes.c_int, [ctypes.POINTER(CsxCfg), ctypes.POINTER(CsxModel),
                                          ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, _u64,
                                          ctypes.c_void_p, ctypes.c_void_p]),
+    "csx_screen_device_noalloc": (ctypes.c_int, [ctypes.POINTER(CsxCfg), ctypes.POINTER(CsxModel),
+                                                 ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, _u64,
+                                                 ctypes.c_void_p, ctypes.c_void_p]),
     "csx_screen_cli": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_char_p)]),
     "csx_limits": (ctypes.c_int, [ctypes.POINTER(_u64), ctypes.POINTER(_u64)]),
     "csx_last_run_info": (ctypes.c_int, [ctypes.POINTER(CsxRunInfo)]),

@@ -973,3 +973,239 @@ int csx_screen(const csx_cfg *cfg, const csx_model *model, const csx_genome *eli
 }
 
 }  // extern "C"
+
+// ---- screen without allocation -----------------------------------------------
+//
+// csx_screen_device_noalloc: the same pipeline with every piece of device
+// scratch carved from one static array compiled into this library, for
+// callers that cannot call cudaMalloc: a process whose memory pool owns the
+// whole device, or a caller that cannot afford the implicit device-wide
+// synchronisation cudaMalloc / cudaFree can bring while its other streams run.
+// The array is process-wide, so calls that overlap on the GPU race; the
+// control block that must start at zero is cleared on every call.
+namespace csx {
+
+constexpr size_t kNoAllocScratchBytes = 32ull << 20;  // held by every GPU that loads the library
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+struct NoAllocDevice {
+    unsigned char *scratch = nullptr;  // device address of g_noalloc_scratch
+    int num_sms = 0;
+    size_t max_smem = 0;
+};
+static std::mutex g_noalloc_mu;
+static NoAllocDevice g_noalloc[64];
+
+// Once per device, with that device current: the scratch's device address.
+// In host code g_noalloc_scratch names a host-side stand-in, never passed on.
+int noalloc_setup(int dev, NoAllocDevice **out) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    NoAllocDevice &d = g_noalloc[dev];
+    if (!d.scratch) {
+        void *p = nullptr;
+        CSX_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        int v = 0;
+        CSX_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
+        d.num_sms = v;
+        CSX_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        d.max_smem = static_cast<size_t>(v);
+        d.scratch = static_cast<unsigned char *>(p);
+    }
+    *out = &d;
+    return CSX_OK;
+}
+
+// Plan for the fixed scratch: items of at least 16384 candidates (fewer items
+// and checkpoints). A segment's range of cnt candidates holds at most
+// ceil(cnt / D) split points, so items <= 2 * segments + lambda / D.
+int plan_noalloc(const NoAllocDevice &dv, const csx_cfg &cfg, int ne, Plan *pl) {
+    StreamGeom &g = pl->g;
+    g.seed = cfg.seed;
+    g.T = std::max<uint64_t>(1, std::min<uint64_t>(cfg.threads, cfg.lambda));
+    g.per = cfg.lambda / g.T;
+    g.my_last = cfg.lambda - (g.T - 1) * g.per;
+    const uint64_t my_max = std::max(g.per, g.my_last);
+    if (g.T >= 0xFFFFFFFFull) return CSX_ERR_LIMIT;
+    pl->fast_delta = std::isfinite(cfg.sigma) && std::fabs(cfg.sigma) <= 1.0e38f;
+    pl->kpad = std::max<uint32_t>(32, pow2_at_least(cfg.keep));
+    pl->sort_n = pow2_at_least(pl->kpad + 2ull * kRounds * kThreads);
+    pl->buf_cap = pl->sort_n - pl->kpad;
+    pl->smem = static_cast<size_t>(pl->sort_n) * sizeof(Entry) +
+               static_cast<size_t>(ne + 1) * kNtot * sizeof(float);
+    if (pl->smem + 1024 > dv.max_smem) return CSX_ERR_LIMIT;
+    int nb = 0;
+    if (pl->fast_delta) {
+        CSX_CUDA(cudaFuncSetAttribute(screen_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(pl->smem)));
+        CSX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, screen_kernel<true>, kThreads, pl->smem));
+    } else {
+        CSX_CUDA(cudaFuncSetAttribute(screen_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(pl->smem)));
+        CSX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, screen_kernel<false>, kThreads, pl->smem));
+    }
+    pl->grid = std::max(1, nb) * dv.num_sms;
+    const uint64_t target = 8ull * static_cast<uint64_t>(pl->grid) * kThreads;
+    uint64_t d = std::max<uint64_t>(16384, cfg.lambda / target);
+    d = std::min<uint64_t>(d, 1ull << 20);
+    uint32_t dl = 0;
+    while ((2ull << dl) <= d) ++dl;
+    g.d_log2 = dl;
+    const uint64_t D = 1ull << dl;
+    const uint32_t it = unit_threshold(cfg.imm_p), jt = unit_threshold(cfg.jump_p);
+    uint64_t gran = 2;
+    if ((it == 0 || it == (1u << 24)) && (jt == 0 || jt == (1u << 24)))
+        gran = (it ? 33 : 62) + (jt ? 2 : 0);
+    uint64_t L = 64 * std::min<uint64_t>(kDefaultSegCands, my_max);
+    L = ((L + gran - 1) / gran) * gran;
+    g.L = L;
+    g.C = static_cast<uint32_t>(std::max<uint64_t>(1, (64 * g.per + L - 1) / L));
+    g.C_last = static_cast<uint32_t>(std::max<uint64_t>(1, (64 * g.my_last + L - 1) / L));
+    g.n_seg = (g.T - 1) * g.C + g.C_last;
+    g.ckcap = static_cast<uint32_t>((L / 33) / D + 3);
+    pl->short_path = my_max <= D;
+    pl->items_cap = pl->short_path ? g.T : 2 * g.n_seg + cfg.lambda / D + 1;
+    if (pl->items_cap >= 0xFFFFFFFFull) return CSX_ERR_LIMIT;
+    return CSX_OK;
+}
+
+// Bump carving of the static scratch (256-byte aligned pieces).
+struct Carve {
+    unsigned char *base;
+    size_t off = 0;
+    template <typename T>
+    T *take(size_t count) {
+        off = (off + 255) & ~static_cast<size_t>(255);
+        T *p = reinterpret_cast<T *>(base + off);
+        off += count * sizeof(T);
+        return p;
+    }
+};
+
+int enqueue_screen_noalloc(const NoAllocDevice &dv, const csx_cfg &cfg, const csx_model &model,
+                           const csx_genome *d_genomes, int ne, csx_survivor *d_out,
+                           unsigned long long *d_result, cudaStream_t st) {
+    Plan pl;
+    int rc = plan_noalloc(dv, cfg, ne, &pl);
+    if (rc) return rc;
+    const StreamGeom &g = pl.g;
+    const bool fast = pl.fast_delta;
+    const uint32_t nl = static_cast<uint32_t>(pl.grid);
+    Carve cv{dv.scratch};
+    Ctrl *ctrl = cv.take<Ctrl>(1);
+    float *tab = cv.take<float>(static_cast<size_t>(ne + 1) * kNtot);
+    auto *ids = cv.take<unsigned long long>(static_cast<size_t>(ne));
+    auto *tribes = cv.take<unsigned int>(static_cast<size_t>(ne));
+    Item *items = cv.take<Item>(pl.items_cap);
+    Entry *lists_a = cv.take<Entry>(static_cast<size_t>(nl) * pl.kpad);
+    Entry *lists_b = cv.take<Entry>(static_cast<size_t>((nl + 1) / 2) * pl.kpad);
+    SegRec *recs = nullptr;
+    uint64_t *ck = nullptr;
+    SegOut *so = nullptr;
+    uint32_t *off = nullptr;
+    if (!pl.short_path) {
+        recs = cv.take<SegRec>(g.n_seg);
+        ck = cv.take<uint64_t>(g.n_seg * g.ckcap);
+        so = cv.take<SegOut>(g.n_seg);
+        off = cv.take<uint32_t>(g.n_seg);
+    }
+    if (cv.off > kNoAllocScratchBytes) {
+        std::fprintf(stderr,
+                     "csx_screen_device_noalloc: this configuration needs %zu bytes of device scratch; "
+                     "the library's static scratch holds %zu\n",
+                     cv.off, kNoAllocScratchBytes);
+        return CSX_ERR_LIMIT;
+    }
+    CSX_CUDA(cudaMemsetAsync(ctrl, 0, sizeof(Ctrl), st));
+    SynthConst sc;
+    sc.ne = static_cast<uint32_t>(ne);
+    sc.ne_magic = ~0ull / static_cast<uint64_t>(ne) + 1;
+    sc.imm_thr = unit_threshold(cfg.imm_p);
+    sc.jump_thr = unit_threshold(cfg.jump_p);
+    sc.sigma = cfg.sigma;
+    sc.nsig1 = -cfg.sigma;
+    sc.nsig2 = -2.0f * cfg.sigma;
+    prep_elites_kernel<<<unit_blocks(static_cast<uint64_t>(ne + 1) * kNtot, 256), 256, 0, st>>>(
+        d_genomes, ne, tab, ids, tribes);
+    CSX_CUDA(cudaGetLastError());
+    if (pl.short_path) {
+        stream_items_kernel<<<unit_blocks(g.T, 256), 256, 0, st>>>(g, items, ctrl);
+        CSX_CUDA(cudaGetLastError());
+    } else {
+        walk_kernel<<<unit_blocks(g.n_seg, 128), 128, 0, st>>>(sc, g, recs, ck, ctrl);
+        CSX_CUDA(cudaGetLastError());
+        assemble_kernel<<<unit_blocks(g.T, 128), 128, 0, st>>>(g, recs, so, ctrl);
+        CSX_CUDA(cudaGetLastError());
+        scan_kernel<<<1, 1024, 0, st>>>(so, g.n_seg, off, ctrl, pl.items_cap);
+        CSX_CUDA(cudaGetLastError());
+        emit_kernel<<<unit_blocks(g.n_seg, 128), 128, 0, st>>>(g, so, off, ck, items, ctrl);
+        CSX_CUDA(cudaGetLastError());
+    }
+    ScreenArgs A;
+    A.m.w0 = model.w0;
+    for (int k = 0; k < kNtot; ++k) A.m.wlin[k] = model.w_lin[k];
+    for (int i = 0; i < 16; ++i)
+        for (int j = 0; j <= i; ++j) A.m.wq[tri(i, j)] = model.w_quad[i * 16 + j];
+    A.sc = sc;
+    A.seed = cfg.seed;
+    A.el = tab;
+    A.items = items;
+    A.ctrl = ctrl;
+    A.lists = lists_a;
+    A.keep = static_cast<uint32_t>(cfg.keep);
+    A.kpad = pl.kpad;
+    A.sort_n = pl.sort_n;
+    A.buf_cap = pl.buf_cap;
+    if (fast)
+        screen_kernel<true><<<pl.grid, kThreads, pl.smem, st>>>(A);
+    else
+        screen_kernel<false><<<pl.grid, kThreads, pl.smem, st>>>(A);
+    CSX_CUDA(cudaGetLastError());
+    const size_t msmem = 2ull * pl.kpad * sizeof(Entry);
+    CSX_CUDA(cudaFuncSetAttribute(merge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(msmem)));
+    Entry *cur = lists_a, *nxt = lists_b;
+    uint32_t n = nl;
+    while (n > 1) {
+        const uint32_t m = (n + 1) / 2;
+        merge_kernel<<<m, 256, msmem, st>>>(cur, n, nxt, pl.kpad);
+        CSX_CUDA(cudaGetLastError());
+        std::swap(cur, nxt);
+        n = m;
+    }
+    if (fast)
+        regen_kernel<true><<<unit_blocks(cfg.keep, 128), 128, 0, st>>>(A, cur, ids, tribes, d_out, d_result);
+    else
+        regen_kernel<false><<<unit_blocks(cfg.keep, 128), 128, 0, st>>>(A, cur, ids, tribes, d_out, d_result);
+    CSX_CUDA(cudaGetLastError());
+    result_kernel<<<1, 32, 0, st>>>(ctrl, d_result);
+    CSX_CUDA(cudaGetLastError());
+    return CSX_OK;
+}
+
+}  // namespace csx
+
+extern "C" int csx_screen_device_noalloc(const csx_cfg *cfg, const csx_model *model,
+                                         const csx_genome *d_elites, int n_elites, csx_survivor *d_out,
+                                         uint64_t out_cap, uint64_t *d_result, void *cuda_stream) {
+    int rc = check_common(cfg, model, n_elites);
+    if (rc) return rc;
+    if (!d_elites || !d_result || (!d_out && cfg->lambda > 0)) return CSX_ERR_BAD_ARGS;
+    if (out_cap < std::min<uint64_t>(cfg->keep, cfg->lambda)) return CSX_ERR_BAD_ARGS;
+    int count = 0, dev = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return CSX_ERR_NO_DEVICE;
+    }
+    CSX_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return CSX_ERR_LIMIT;
+    NoAllocDevice *dv = nullptr;
+    rc = noalloc_setup(dev, &dv);
+    if (rc) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+    if (cfg->lambda == 0) {
+        CSX_CUDA(cudaMemsetAsync(d_result, 0, 4 * sizeof(uint64_t), st));
+        return CSX_OK;
+    }
+    return enqueue_screen_noalloc(*dv, *cfg, *model, d_elites, n_elites, d_out,
+                                  reinterpret_cast<unsigned long long *>(d_result), st);
+}

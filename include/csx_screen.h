@@ -145,6 +145,22 @@ int csx_screen_device(const csx_cfg *cfg, const csx_model *model, const csx_geno
                       int n_elites, csx_survivor *d_out, uint64_t out_cap, uint64_t *d_result,
                       void *cuda_stream);
 
+/* No counterpart in the reference. csx_screen_device for callers that cannot
+ * allocate device memory: a process whose own memory pool owns the whole
+ * device, or a caller that cannot afford the implicit device-wide
+ * synchronisation of cudaMalloc / cudaFree while its other streams run. This
+ * call allocates nothing: its scratch is a 32 MiB array compiled into the
+ * library, which every GPU that loads the library holds until the process
+ * exits. Configurations needing more scratch return CSX_ERR_LIMIT with a
+ * message naming the bytes needed (the 2.65e9-candidate, T = 4, keep 256
+ * generation needs about 19 MiB). The first call on a device looks up the
+ * array's device address; make that first call before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race, so order
+ * them (one stream, or events). Results equal csx_screen_device's. */
+int csx_screen_device_noalloc(const csx_cfg *cfg, const csx_model *model, const csx_genome *d_elites,
+                              int n_elites, csx_survivor *d_out, uint64_t out_cap, uint64_t *d_result,
+                              void *cuda_stream);
+
 /* The `arena screen` verb, src/main.zig:156-218 plus run()'s file output
  * (src/screen.zig:321-342): argv holds the flags after "screen". Returns 0
  * or a negative status; a message is printed to stderr on failure. */
