@@ -29,6 +29,7 @@ constexpr int kNq = 136;  // lower-triangular quad terms over the 16 legacy gene
 // Model in the compact triangular form used on the device.
 struct DevModel {
     float w0;
+    float w16;  // 16 * w0 (exact): the intercept as Model.score counts it
     float wlin[kNtot];
     float wq[kNq];  // (i, j <= i) at i*(i+1)/2 + j  ==  Model.w_quad[i*16 + j]
 };
@@ -121,7 +122,13 @@ __device__ __forceinline__ CandHead cand_head(const SynthConst &C, uint64_t seed
 // exact, so this is one rounding of (y-c)*B == round((u-0.5)*2*B). Valid for
 // finite |B| <= 1e38 (then |delta| < |B| is finite too); otherwise the
 // two-op form is used.
-template <bool kFastDelta, bool kKeepGenes>
+//
+// kExact = false computes a filter score instead: the same surface by FFMA
+// Horner, t_l = w_l + sum_{i>=l} Wq[i][l] g_i, s = 16 w0 + sum_l g_l t_l +
+// sum_{k>=16} w_k g_k (165 FFMA). Both orders are within gamma_n * A of the
+// real value (A = sum of |terms|), so the host bounds |fast - exact| and the
+// exact order is evaluated only for candidates the bound cannot rule out.
+template <bool kFastDelta, bool kKeepGenes, bool kExact = true>
 __device__ __forceinline__ float synth_score(const DevModel &M, const SynthConst &C,
                                              const float *__restrict__ el, uint64_t seed_t,
                                              uint64_t p, const CandHead &h, float *genes) {
@@ -137,7 +144,7 @@ __device__ __forceinline__ float synth_score(const DevModel &M, const SynthConst
     uint64_t su = s0 + (h.imm ? 3ull : 4ull) * kGolden;  // unit draw of gene 0
 
     float G[16], S[16];
-    float R = 0.0f;
+    float R = kExact ? 0.0f : M.w16;
 #pragma unroll
     for (int k = 0; k < kNtot; ++k) {
         const uint32_t bw = draw_bitword(su - kGolden);  // crossover bit draw
@@ -162,7 +169,16 @@ __device__ __forceinline__ float synth_score(const DevModel &M, const SynthConst
             g = (g != g) ? 1.0f : fmaxf(fminf(g, 1.0f), 0.0f);
         g = (static_cast<uint32_t>(k) == h.jidx) ? h.jval : g;
         if (kKeepGenes) genes[k] = g;
-        if (k < 16) {
+        if (!kExact) {
+            if (k < 16) {
+                G[k] = g;
+#pragma unroll
+                for (int l = 0; l < k; ++l) S[l] = __fmaf_rn(M.wq[tri(k, l)], g, S[l]);
+                S[k] = __fmaf_rn(M.wq[tri(k, k)], g, M.wlin[k]);
+            } else {
+                R = __fmaf_rn(M.wlin[k], g, R);
+            }
+        } else if (k < 16) {
             G[k] = g;
 #pragma unroll
             for (int l = 0; l < k; ++l)
@@ -172,6 +188,11 @@ __device__ __forceinline__ float synth_score(const DevModel &M, const SynthConst
             const float t = __fmul_rn(M.wlin[k], g);
             R = (k == 16) ? __fadd_rn(0.0f, t) : __fadd_rn(R, t);
         }
+    }
+    if (!kExact) {
+#pragma unroll
+        for (int l = 0; l < 16; ++l) R = __fmaf_rn(G[l], S[l], R);
+        return R;
     }
     float r = __fadd_rn(__fadd_rn(M.w0, __fmul_rn(M.wlin[0], G[0])), S[0]);
 #pragma unroll

@@ -181,17 +181,17 @@ __global__ void walk_kernel(SynthConst sc, StreamGeom g, SegRec *__restrict__ re
     uint64_t q = e, kb = 0, steps = 0;
     r.status = kSegOk;
     while (p != q) {
-        if (p < q) {
-            if ((k & dmask) == 0) {
-                const uint64_t m = k >> g.d_log2;
-                if (m < g.ckcap) ckp[m] = p;
-            }
-            p = walk_step(sc, seed_t, p);
-            ++k;
-        } else {
-            q = walk_step(sc, seed_t, q);
-            ++kb;
+        // advance whichever chain is behind: one step per iteration, no divergence
+        const bool a = p < q;
+        if (a && (k & dmask) == 0) {
+            const uint64_t m = k >> g.d_log2;
+            if (m < g.ckcap) ckp[m] = p;
         }
+        const uint64_t y = walk_step(sc, seed_t, a ? p : q);
+        p = a ? y : p;
+        q = a ? q : y;
+        k += a;
+        kb += !a;
         if (++steps > kLinkCap) {
             r.status = kSegFail;
             atomicOr(&ctrl->err, kErrLink);
@@ -246,6 +246,129 @@ __global__ void assemble_kernel(StreamGeom g, const SegRec *__restrict__ recs, S
         }
     }
     if (idx != my) atomicOr(&ctrl->err, kErrAssemble);
+}
+
+// One CTA per stream. Segment c's truth range starts where link c-1 met
+// (lo = b_next of c-1, pos = its merge_pos) unless that meeting lies before
+// the truth reached chain c-1 (lo > hi there); the block checks every segment
+// for that case and, if it occurs (rare), falls back to the sequential loop.
+constexpr int kAsmThreads = 256;
+
+__global__ void __launch_bounds__(kAsmThreads) assemble_block_kernel(StreamGeom g,
+                                                                      const SegRec *__restrict__ recs,
+                                                                      SegOut *__restrict__ outs,
+                                                                      Ctrl *__restrict__ ctrl) {
+    __shared__ unsigned long long wsum[kAsmThreads / 32];
+    __shared__ unsigned long long carry;
+    __shared__ int irregular;
+    const uint64_t t = blockIdx.x;
+    const bool last_stream = t == g.T - 1;
+    const uint64_t my = last_stream ? g.my_last : g.per;
+    const uint32_t ct = last_stream ? g.C_last : g.C;
+    const uint64_t s0 = t * g.C;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (tid == 0) {
+        carry = 0;
+        irregular = 0;
+    }
+    __syncthreads();
+    for (uint32_t base = 0; base < ct; base += kAsmThreads) {
+        const uint32_t c = base + tid;
+        uint64_t lo = 0, pos = 0, len = 0, hi = 0;
+        bool bad = false;
+        if (c < ct) {
+            const SegRec r = recs[s0 + c];
+            if (c > 0) {
+                const SegRec q = recs[s0 + c - 1];
+                lo = q.b_next;
+                pos = q.merge_pos;
+                bad |= q.status == kSegFail;
+            }
+            hi = (r.status == kSegLast) ? r.n : static_cast<uint64_t>(r.n) + r.a;
+            bad |= r.status == kSegFail || lo > hi;
+            len = hi > lo ? hi - lo : 0;
+        }
+        if (__syncthreads_or(bad)) {
+            if (tid == 0) irregular = 1;
+            break;
+        }
+        // block exclusive scan of len
+        unsigned long long v = len;
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long u = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += u;
+        }
+        if (lane == 31) wsum[w] = v;
+        __syncthreads();
+        if (w == 0) {
+            unsigned long long x = lane < kAsmThreads / 32 ? wsum[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned long long u = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += u;
+            }
+            if (lane < kAsmThreads / 32) wsum[lane] = x;
+        }
+        __syncthreads();
+        const unsigned long long idx = carry + (w > 0 ? wsum[w - 1] : 0ull) + v - len;
+        if (c < ct) {
+            SegOut o;
+            o.pos = pos;
+            o.I = idx < my ? idx : my;
+            o.lo = lo;
+            o.cnt = 0;
+            o.nitems = 0;
+            if (idx < my && len > 0) {
+                const uint64_t cnt = len < my - idx ? len : my - idx;
+                uint64_t mmin, mmax;
+                split_range(lo, cnt, g.d_log2, g.ckcap, mmin, mmax);
+                o.cnt = static_cast<uint32_t>(cnt);
+                o.nitems = 1 + (mmax >= mmin ? static_cast<uint32_t>(mmax - mmin + 1) : 0u);
+            }
+            outs[s0 + c] = o;
+        }
+        __syncthreads();
+        if (tid == kAsmThreads - 1) carry += wsum[kAsmThreads / 32 - 1];
+        __syncthreads();
+    }
+    __syncthreads();
+    if (irregular) {
+        if (tid == 0) {  // sequential: follows the truth through late meetings
+            uint64_t lo = 0, pos = 0, idx = 0;
+            bool bad = false;
+            for (uint32_t c = 0; c < ct; ++c) {
+                const SegRec r = recs[s0 + c];
+                SegOut o;
+                o.pos = pos;
+                o.I = idx;
+                o.lo = lo;
+                o.cnt = 0;
+                o.nitems = 0;
+                if (r.status == kSegFail) bad = true;
+                const uint64_t hi = (r.status == kSegLast) ? r.n : static_cast<uint64_t>(r.n) + r.a;
+                if (!bad && idx < my && hi > lo) {
+                    uint64_t cnt = hi - lo;
+                    if (cnt > my - idx) cnt = my - idx;
+                    uint64_t mmin, mmax;
+                    split_range(lo, cnt, g.d_log2, g.ckcap, mmin, mmax);
+                    o.cnt = static_cast<uint32_t>(cnt);
+                    o.nitems = 1 + (mmax >= mmin ? static_cast<uint32_t>(mmax - mmin + 1) : 0u);
+                    idx += cnt;
+                }
+                outs[s0 + c] = o;
+                if (r.status == kSegOk) {
+                    if (hi >= lo) {
+                        lo = r.b_next;
+                        pos = r.merge_pos;
+                    } else {
+                        lo = r.b_next + (lo - hi);
+                    }
+                }
+            }
+            if (idx != my) atomicOr(&ctrl->err, kErrAssemble);
+        }
+    } else if (tid == 0 && carry < my) {
+        atomicOr(&ctrl->err, kErrAssemble);
+    }
 }
 
 // ---- 3. scan + emit ---------------------------------------------------------------
@@ -353,6 +476,7 @@ struct ScreenArgs {
     Ctrl *ctrl;
     Entry *lists;     // gridDim.x x kpad
     uint32_t keep, kpad, sort_n, buf_cap;
+    float err;        // bound on |filter score - exact score| (filter mode)
 };
 
 // Bitonic sort of E[0..n) (n a power of two), best entry first.
@@ -374,7 +498,19 @@ __device__ void cta_sort_desc(Entry *E, uint32_t n) {
     }
 }
 
+// The reference-order score of one candidate, out of line: it runs only for
+// candidates the filter cannot rule out, and keeping it out of the caller
+// stops the compiler from holding both evaluations' values live at once.
 template <bool kFastDelta>
+__device__ __noinline__ float exact_score_at(const ScreenArgs *__restrict__ A, const float *el,
+                                             uint64_t seed_t, uint64_t p) {
+    const CandHead h = cand_head(A->sc, seed_t, p);
+    return synth_score<kFastDelta, false, true>(A->m, A->sc, el, seed_t, p, h, nullptr);
+}
+
+// kFilter: score with the FFMA filter form and evaluate the reference's f32
+// order only when the filter score is within A.err of the threshold.
+template <bool kFastDelta, bool kFilter>
 __global__ void __launch_bounds__(kThreads) screen_kernel(const __grid_constant__ ScreenArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Entry *E = reinterpret_cast<Entry *>(smem_raw);
@@ -440,10 +576,17 @@ __global__ void __launch_bounds__(kThreads) screen_kernel(const __grid_constant_
             t2 = 0;
             ts = okey_score(gk);
         }
+        const float tlo = kFilter ? __fsub_rd(ts, A.err) : ts;
 #pragma unroll 1
         for (int r = 0; r < kRounds && valid; ++r) {
             const CandHead h = cand_head(A.sc, seed_t, p);
-            const float s = synth_score<kFastDelta, false>(A.m, A.sc, el, seed_t, p, h, nullptr);
+            float s;
+            if (kFilter) {
+                s = synth_score<kFastDelta, false, false>(A.m, A.sc, el, seed_t, p, h, nullptr);
+                s = (s >= tlo) ? exact_score_at<kFastDelta>(&A, el, seed_t, p) : -INFINITY;
+            } else {
+                s = synth_score<kFastDelta, false>(A.m, A.sc, el, seed_t, p, h, nullptr);
+            }
             if (s >= ts) {
                 const unsigned long long k1 =
                     (static_cast<unsigned long long>(score_okey(s)) << 32) | static_cast<unsigned int>(~item);
@@ -634,6 +777,8 @@ struct Plan {
     int grid = 0;
     size_t smem = 0;
     bool fast_delta = true;
+    bool filter = false;
+    float err = 0.0f;
 };
 
 int context_init(Context &cx, int dev) {
@@ -649,17 +794,41 @@ int context_init(Context &cx, int dev) {
     return CSX_OK;
 }
 
-template <bool kFast>
-int occupancy(const Context &cx, size_t smem, int *blocks) {
-    CSX_CUDA(cudaFuncSetAttribute(screen_kernel<kFast>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  static_cast<int>(smem)));
+using ScreenFn = void (*)(ScreenArgs);
+
+ScreenFn screen_fn(bool fast_delta, bool filter) {
+    if (fast_delta) return filter ? screen_kernel<true, true> : screen_kernel<true, false>;
+    return filter ? screen_kernel<false, true> : screen_kernel<false, false>;
+}
+
+int screen_occupancy(ScreenFn fn, int num_sms, size_t smem, int *blocks) {
+    CSX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     int nb = 0;
-    CSX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, screen_kernel<kFast>, kThreads, smem));
-    *blocks = std::max(1, nb) * cx.num_sms;
+    CSX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kThreads, smem));
+    *blocks = std::max(1, nb) * num_sms;
     return CSX_OK;
 }
 
-int make_plan(const Context &cx, const csx_cfg &cfg, int ne, Plan *pl) {
+// Bound on |filter score - exact score| for genes in [0, 1]: the exact
+// order puts each term through at most 35 roundings (2 products, 16 lane
+// adds, the lane total, 15 reduction adds, the tail add), the FFMA form
+// through at most 47 (16 Horner steps, 30 outer steps, slack one); a sum of
+// terms evaluated with at most n roundings per term is within
+// gamma_n * sum|terms| (gamma_n = n u / (1 - n u), u = 2^-24) of the real sum.
+// Returns 0 when the filter cannot be used (non-finite or huge weights).
+float filter_bound(const csx_model &m) {
+    double a = 16.0 * std::fabs(static_cast<double>(m.w0));
+    for (int k = 0; k < kNtot; ++k) a += std::fabs(static_cast<double>(m.w_lin[k]));
+    for (int i = 0; i < 16; ++i)
+        for (int j = 0; j <= i; ++j) a += std::fabs(static_cast<double>(m.w_quad[i * 16 + j]));
+    if (!std::isfinite(a) || a > 1e30) return 0.0f;
+    const double u = std::ldexp(1.0, -24);
+    auto gamma = [u](double n) { return n * u / (1.0 - n * u); };
+    const double e = (gamma(35) + gamma(47)) * a * (1.0 + std::ldexp(1.0, -20)) + 1e-30;
+    return std::nextafter(static_cast<float>(e), INFINITY);
+}
+
+int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int ne, Plan *pl) {
     StreamGeom &g = pl->g;
     g.seed = cfg.seed;
     g.T = std::max<uint64_t>(1, std::min<uint64_t>(cfg.threads, cfg.lambda));  // src/screen.zig:267
@@ -668,6 +837,8 @@ int make_plan(const Context &cx, const csx_cfg &cfg, int ne, Plan *pl) {
     const uint64_t my_max = std::max(g.per, g.my_last);
     if (g.T >= 0xFFFFFFFFull) return CSX_ERR_LIMIT;
     pl->fast_delta = std::isfinite(cfg.sigma) && std::fabs(cfg.sigma) <= 1.0e38f;
+    pl->err = filter_bound(model);
+    pl->filter = !(cfg.flags & CSX_FLAG_EXACT_ALL) && pl->err > 0.0f;
 
     pl->kpad = std::max<uint32_t>(32, pow2_at_least(cfg.keep));
     pl->sort_n = pow2_at_least(pl->kpad + 2ull * kRounds * kThreads);
@@ -675,8 +846,7 @@ int make_plan(const Context &cx, const csx_cfg &cfg, int ne, Plan *pl) {
     pl->smem = static_cast<size_t>(pl->sort_n) * sizeof(Entry) +
                static_cast<size_t>(ne + 1) * kNtot * sizeof(float);
     if (pl->smem + 1024 > cx.max_smem) return CSX_ERR_LIMIT;
-    int rc = pl->fast_delta ? occupancy<true>(cx, pl->smem, &pl->grid)
-                            : occupancy<false>(cx, pl->smem, &pl->grid);
+    int rc = screen_occupancy(screen_fn(pl->fast_delta, pl->filter), cx.num_sms, pl->smem, &pl->grid);
     if (rc) return rc;
 
     // item size D: about eight items per screen thread
@@ -716,7 +886,7 @@ int unit_blocks(uint64_t n, int threads) { return static_cast<int>((n + threads 
 int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, const csx_genome *d_genomes,
                    int ne, csx_survivor *d_out, unsigned long long *d_result, cudaStream_t st) {
     Plan pl;
-    int rc = make_plan(cx, cfg, ne, &pl);
+    int rc = make_plan(cx, cfg, model, ne, &pl);
     if (rc) return rc;
     const StreamGeom &g = pl.g;
     const bool fast = pl.fast_delta;
@@ -778,7 +948,10 @@ int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, cons
         auto *off = static_cast<uint32_t *>(cx.off.p);
         walk_kernel<<<unit_blocks(g.n_seg, 128), 128, 0, st>>>(sc, g, recs, ck, ctrl);
         CSX_CUDA(cudaGetLastError());
-        assemble_kernel<<<unit_blocks(g.T, 128), 128, 0, st>>>(g, recs, so, ctrl);
+        if (g.C >= 64)
+            assemble_block_kernel<<<static_cast<unsigned>(g.T), kAsmThreads, 0, st>>>(g, recs, so, ctrl);
+        else
+            assemble_kernel<<<unit_blocks(g.T, 128), 128, 0, st>>>(g, recs, so, ctrl);
         CSX_CUDA(cudaGetLastError());
         scan_kernel<<<1, 1024, 0, st>>>(so, g.n_seg, off, ctrl, pl.items_cap);
         CSX_CUDA(cudaGetLastError());
@@ -790,6 +963,7 @@ int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, cons
 
     ScreenArgs A;
     A.m.w0 = model.w0;
+    A.m.w16 = 16.0f * model.w0;
     for (int k = 0; k < kNtot; ++k) A.m.wlin[k] = model.w_lin[k];
     for (int i = 0; i < 16; ++i)
         for (int j = 0; j <= i; ++j) A.m.wq[tri(i, j)] = model.w_quad[i * 16 + j];
@@ -803,10 +977,8 @@ int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, cons
     A.kpad = pl.kpad;
     A.sort_n = pl.sort_n;
     A.buf_cap = pl.buf_cap;
-    if (fast)
-        screen_kernel<true><<<pl.grid, kThreads, pl.smem, st>>>(A);
-    else
-        screen_kernel<false><<<pl.grid, kThreads, pl.smem, st>>>(A);
+    A.err = pl.err;
+    screen_fn(fast, pl.filter)<<<pl.grid, kThreads, pl.smem, st>>>(A);
     CSX_CUDA(cudaGetLastError());
     ++launches;
     CSX_CUDA(mark(3));
@@ -1018,7 +1190,7 @@ int noalloc_setup(int dev, NoAllocDevice **out) {
 // Plan for the fixed scratch: items of at least 16384 candidates (fewer items
 // and checkpoints). A segment's range of cnt candidates holds at most
 // ceil(cnt / D) split points, so items <= 2 * segments + lambda / D.
-int plan_noalloc(const NoAllocDevice &dv, const csx_cfg &cfg, int ne, Plan *pl) {
+int plan_noalloc(const NoAllocDevice &dv, const csx_cfg &cfg, const csx_model &model, int ne, Plan *pl) {
     StreamGeom &g = pl->g;
     g.seed = cfg.seed;
     g.T = std::max<uint64_t>(1, std::min<uint64_t>(cfg.threads, cfg.lambda));
@@ -1027,23 +1199,16 @@ int plan_noalloc(const NoAllocDevice &dv, const csx_cfg &cfg, int ne, Plan *pl) 
     const uint64_t my_max = std::max(g.per, g.my_last);
     if (g.T >= 0xFFFFFFFFull) return CSX_ERR_LIMIT;
     pl->fast_delta = std::isfinite(cfg.sigma) && std::fabs(cfg.sigma) <= 1.0e38f;
+    pl->err = filter_bound(model);
+    pl->filter = !(cfg.flags & CSX_FLAG_EXACT_ALL) && pl->err > 0.0f;
     pl->kpad = std::max<uint32_t>(32, pow2_at_least(cfg.keep));
     pl->sort_n = pow2_at_least(pl->kpad + 2ull * kRounds * kThreads);
     pl->buf_cap = pl->sort_n - pl->kpad;
     pl->smem = static_cast<size_t>(pl->sort_n) * sizeof(Entry) +
                static_cast<size_t>(ne + 1) * kNtot * sizeof(float);
     if (pl->smem + 1024 > dv.max_smem) return CSX_ERR_LIMIT;
-    int nb = 0;
-    if (pl->fast_delta) {
-        CSX_CUDA(cudaFuncSetAttribute(screen_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      static_cast<int>(pl->smem)));
-        CSX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, screen_kernel<true>, kThreads, pl->smem));
-    } else {
-        CSX_CUDA(cudaFuncSetAttribute(screen_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      static_cast<int>(pl->smem)));
-        CSX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, screen_kernel<false>, kThreads, pl->smem));
-    }
-    pl->grid = std::max(1, nb) * dv.num_sms;
+    int rc = screen_occupancy(screen_fn(pl->fast_delta, pl->filter), dv.num_sms, pl->smem, &pl->grid);
+    if (rc) return rc;
     const uint64_t target = 8ull * static_cast<uint64_t>(pl->grid) * kThreads;
     uint64_t d = std::max<uint64_t>(16384, cfg.lambda / target);
     d = std::min<uint64_t>(d, 1ull << 20);
@@ -1085,7 +1250,7 @@ int enqueue_screen_noalloc(const NoAllocDevice &dv, const csx_cfg &cfg, const cs
                            const csx_genome *d_genomes, int ne, csx_survivor *d_out,
                            unsigned long long *d_result, cudaStream_t st) {
     Plan pl;
-    int rc = plan_noalloc(dv, cfg, ne, &pl);
+    int rc = plan_noalloc(dv, cfg, model, ne, &pl);
     if (rc) return rc;
     const StreamGeom &g = pl.g;
     const bool fast = pl.fast_delta;
@@ -1133,7 +1298,10 @@ int enqueue_screen_noalloc(const NoAllocDevice &dv, const csx_cfg &cfg, const cs
     } else {
         walk_kernel<<<unit_blocks(g.n_seg, 128), 128, 0, st>>>(sc, g, recs, ck, ctrl);
         CSX_CUDA(cudaGetLastError());
-        assemble_kernel<<<unit_blocks(g.T, 128), 128, 0, st>>>(g, recs, so, ctrl);
+        if (g.C >= 64)
+            assemble_block_kernel<<<static_cast<unsigned>(g.T), kAsmThreads, 0, st>>>(g, recs, so, ctrl);
+        else
+            assemble_kernel<<<unit_blocks(g.T, 128), 128, 0, st>>>(g, recs, so, ctrl);
         CSX_CUDA(cudaGetLastError());
         scan_kernel<<<1, 1024, 0, st>>>(so, g.n_seg, off, ctrl, pl.items_cap);
         CSX_CUDA(cudaGetLastError());
@@ -1142,6 +1310,7 @@ int enqueue_screen_noalloc(const NoAllocDevice &dv, const csx_cfg &cfg, const cs
     }
     ScreenArgs A;
     A.m.w0 = model.w0;
+    A.m.w16 = 16.0f * model.w0;
     for (int k = 0; k < kNtot; ++k) A.m.wlin[k] = model.w_lin[k];
     for (int i = 0; i < 16; ++i)
         for (int j = 0; j <= i; ++j) A.m.wq[tri(i, j)] = model.w_quad[i * 16 + j];
@@ -1155,10 +1324,8 @@ int enqueue_screen_noalloc(const NoAllocDevice &dv, const csx_cfg &cfg, const cs
     A.kpad = pl.kpad;
     A.sort_n = pl.sort_n;
     A.buf_cap = pl.buf_cap;
-    if (fast)
-        screen_kernel<true><<<pl.grid, kThreads, pl.smem, st>>>(A);
-    else
-        screen_kernel<false><<<pl.grid, kThreads, pl.smem, st>>>(A);
+    A.err = pl.err;
+    screen_fn(fast, pl.filter)<<<pl.grid, kThreads, pl.smem, st>>>(A);
     CSX_CUDA(cudaGetLastError());
     const size_t msmem = 2ull * pl.kpad * sizeof(Entry);
     CSX_CUDA(cudaFuncSetAttribute(merge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,

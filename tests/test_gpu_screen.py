@@ -255,3 +255,37 @@ def test_screen_device_torch_stream(orc):
     got = screen.survivors_from_bytes(d_out.cpu().numpy(), int(res[0]))
     want, _ = _orc(orc, 150_000, 100, 4, 4, w, el)
     assert_same(got, want)
+
+
+@pytest.mark.parametrize("flags", [0, 8])
+def test_filter_and_exact_modes(orc, flags):
+    """Default mode scores with a certified FFMA filter and re-evaluates the
+    reference order only near the threshold; CSX_FLAG_EXACT_ALL (8) evaluates
+    the reference order for every candidate. Both must equal the oracle."""
+    from codec_arena_gb300 import workloads as wl
+
+    check(orc, 300_000, 256, 17, 4, wl.surrogate_161(), wl.seeded_elites(64), flags=flags)
+
+
+def test_filter_wide_dynamic_range(orc):
+    """Coefficients spanning 1e-6..1e6 with cancelling signs: large rounding
+    differences between the two evaluation orders."""
+    from codec_arena_gb300 import workloads as wl
+
+    rng = np.random.default_rng(3)
+    w = (rng.choice([-1.0, 1.0], 166) * 10.0 ** rng.uniform(-6, 6, 166)).astype(np.float32)
+    w[0] = 1e5
+    for keep in (1, 64):
+        check(orc, 200_000, keep, 5, 4, w, wl.seeded_elites(64))
+
+
+def test_filter_near_ties(orc):
+    """A surface with few distinct values (integer weights, genes snapped by
+    clamping) makes many scores tie or nearly tie at the threshold."""
+    from codec_arena_gb300 import workloads as wl
+
+    w = np.zeros(153, np.float32)
+    w[1:17] = 1.0
+    el = wl.seeded_elites(8)
+    el["g"][:] = np.where(el["g"] > 0.5, 2.0, -1.0)
+    check(orc, 100_000, 200, 3, 4, w, el, sigma=0.1, imm=0.0, jump=0.0)
