@@ -318,6 +318,7 @@ def main():
             "clocks": clocks, "gpu_launches": int(launches * args.steps),
             "stages_ms_last_step": {k: round(v, 4) for k, v in stage[-1].items() if k.startswith("ms_")},
             "shape": {k: stage[-1][k] for k in ("screen_ctas", "segments", "seg_draws", "item_cands")},
+            "exact_evals_last_step": stage[-1]["exact_evals"],
             "wall_s": wall}
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args, args.cpu_seconds)

@@ -61,7 +61,8 @@ class CsxSurvivor(ctypes.Structure):
 class CsxRunInfo(ctypes.Structure):
     _fields_ = [("launches", _u32), ("screen_ctas", _u32), ("segments", _u64), ("seg_draws", _u64),
                 ("item_cands", _u64), ("items", _u64), ("ms_prep", _f32), ("ms_items", _f32),
-                ("ms_screen", _f32), ("ms_merge", _f32), ("ms_regen", _f32), ("ms_total", _f32)]
+                ("ms_screen", _f32), ("ms_merge", _f32), ("ms_regen", _f32), ("ms_total", _f32),
+                ("exact_evals", _u64)]
 
 
 # numpy views with the same layout (bulk conversion without per-field ctypes)
@@ -77,7 +78,7 @@ SURVIVOR_DTYPE = np.dtype({"names": ["score", "tribe", "pa", "pb", "stream", "in
 assert ctypes.sizeof(CsxGenome) == GENOME_DTYPE.itemsize == 152
 assert ctypes.sizeof(CsxSurvivor) == SURVIVOR_DTYPE.itemsize == 168
 assert ctypes.sizeof(CsxCfg) == 48
-assert ctypes.sizeof(CsxRunInfo) == 64
+assert ctypes.sizeof(CsxRunInfo) == 72
 assert ctypes.sizeof(CsxModel) == 4 * (1 + NTOT + 256)
 
 # Every entry point of include/csx_screen.h with its ctypes signature.

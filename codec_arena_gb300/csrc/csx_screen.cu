@@ -89,6 +89,7 @@ struct Ctrl {
     unsigned int n_items;
     unsigned long long screened;
     unsigned long long n_out;
+    unsigned long long exact_evals;  // reference-order evaluations (filter mode)
 };
 
 struct StreamGeom {
@@ -543,7 +544,7 @@ __global__ void __launch_bounds__(kThreads) screen_kernel(const __grid_constant_
         left = it.n;
         valid = left > 0;
     }
-    unsigned long long screened = 0;
+    unsigned long long screened = 0, exact = 0;
     unsigned int gk = 0;
     uint32_t round = 0;
 
@@ -583,7 +584,12 @@ __global__ void __launch_bounds__(kThreads) screen_kernel(const __grid_constant_
             float s;
             if (kFilter) {
                 s = synth_score<kFastDelta, false, false>(A.m, A.sc, el, seed_t, p, h, nullptr);
-                s = (s >= tlo) ? exact_score_at<kFastDelta>(&A, el, seed_t, p) : -INFINITY;
+                if (s >= tlo) {
+                    s = exact_score_at<kFastDelta>(&A, el, seed_t, p);
+                    ++exact;
+                } else {
+                    s = -INFINITY;
+                }
             } else {
                 s = synth_score<kFastDelta, false>(A.m, A.sc, el, seed_t, p, h, nullptr);
             }
@@ -620,8 +626,14 @@ __global__ void __launch_bounds__(kThreads) screen_kernel(const __grid_constant_
     Entry *out = A.lists + static_cast<size_t>(blockIdx.x) * A.kpad;
     for (uint32_t i = tid; i < A.kpad; i += kThreads) out[i] = E[i];
     // screened count: warp reduce then one atomic per warp
-    for (int o = 16; o > 0; o >>= 1) screened += __shfl_down_sync(0xffffffffu, screened, o);
-    if ((tid & 31) == 0) atomicAdd(&A.ctrl->screened, screened);
+    for (int o = 16; o > 0; o >>= 1) {
+        screened += __shfl_down_sync(0xffffffffu, screened, o);
+        exact += __shfl_down_sync(0xffffffffu, exact, o);
+    }
+    if ((tid & 31) == 0) {
+        atomicAdd(&A.ctrl->screened, screened);
+        if (kFilter) atomicAdd(&A.ctrl->exact_evals, exact);
+    }
 }
 
 // ---- 5. merge tree ------------------------------------------------------------------
@@ -1051,6 +1063,9 @@ int csx_last_run_info(csx_run_info *out) {
         float *ms[5] = {&out->ms_prep, &out->ms_items, &out->ms_screen, &out->ms_merge, &out->ms_regen};
         for (int i = 0; i < 5; ++i) CSX_CUDA(cudaEventElapsedTime(ms[i], cx->ev[i], cx->ev[i + 1]));
         CSX_CUDA(cudaEventElapsedTime(&out->ms_total, cx->ev[0], cx->ev[5]));
+        Ctrl c;
+        CSX_CUDA(cudaMemcpy(&c, cx->ctrl.p, sizeof(Ctrl), cudaMemcpyDeviceToHost));
+        out->exact_evals = c.exact_evals;
     }
     return CSX_OK;
 }

@@ -186,6 +186,7 @@ typedef struct csx_run_info {
     float ms_merge;         /* top-K merge tree */
     float ms_regen;         /* survivor regeneration */
     float ms_total;
+    uint64_t exact_evals;   /* candidates scored in the reference order (filter mode) */
 } csx_run_info;
 int csx_last_run_info(csx_run_info *out);
 
