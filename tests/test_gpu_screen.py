@@ -52,11 +52,38 @@ def assert_same(got, want):
     np.testing.assert_array_equal(got["g"].view(np.uint32), want["g"].view(np.uint32))
 
 
-def check(orc, *args, **kw):
+def assert_same_modulo_ties(got, want):
+    """Equal f32 scores from one stream are ordered by the reference's heap
+    array positions and by (stream, index) here; at the boundary score the
+    heap's history also picks which tied candidates survive. Everything else
+    must agree: the score sequence bit for bit, and for every score above the
+    boundary the exact set of candidates."""
+    assert len(got) == len(want)
+    np.testing.assert_array_equal(got["score"].view(np.uint32), want["score"].view(np.uint32))
+    if len(got) == 0:
+        return
+    lowest = got["score"].view(np.uint32)[-1]
+
+    def rows(a):
+        return sorted((int(r["stream"]), int(r["index"]), int(r["draw"]), int(r["pa"]), int(r["pb"]),
+                       int(r["tribe"]), r["g"].tobytes()) for r in a)
+
+    for v in np.unique(got["score"].view(np.uint32)):
+        if v == lowest:
+            continue
+        gs = got[got["score"].view(np.uint32) == v]
+        ws = want[want["score"].view(np.uint32) == v]
+        assert rows(gs) == rows(ws)
+
+
+def check(orc, *args, ties="strict", **kw):
     got, sg = _gpu(*args, **kw)
     want, sw = _orc(orc, *args, **kw)
     assert sg == sw
-    assert_same(got, want)
+    if ties == "strict":
+        assert_same(got, want)
+    else:
+        assert_same_modulo_ties(got, want)
     return got
 
 
@@ -288,4 +315,5 @@ def test_filter_near_ties(orc):
     w[1:17] = 1.0
     el = wl.seeded_elites(8)
     el["g"][:] = np.where(el["g"] > 0.5, 2.0, -1.0)
-    check(orc, 100_000, 200, 3, 4, w, el, sigma=0.1, imm=0.0, jump=0.0)
+    got = check(orc, 100_000, 200, 3, 4, w, el, sigma=0.1, imm=0.0, jump=0.0, ties="aware")
+    assert len(np.unique(got["score"])) < len(got)  # the case really has ties
