@@ -201,18 +201,6 @@ __device__ __forceinline__ float synth_score(const DevModel &M, const SynthConst
     return __fadd_rn(r, R);
 }
 
-// Candidate-start walk: position of the next candidate after the one at p.
-// The draws at p+32 and p+61 (both possible jump tests) are computed beside
-// the immigrant test so the chain advances one hash latency per step.
-__device__ __forceinline__ uint64_t walk_step(const SynthConst &C, uint64_t seed_t, uint64_t p) {
-    const uint64_t s0 = seed_t + (p + 1) * kGolden;
-    const bool imm = (draw_vh(s0 + 2 * kGolden) >> 8) < C.imm_thr;
-    const bool ja = (draw_vh(s0 + 32 * kGolden) >> 8) < C.jump_thr;
-    const bool jb = (draw_vh(s0 + 61 * kGolden) >> 8) < C.jump_thr;
-    const bool jump = imm ? ja : jb;
-    return p + (imm ? 33u : 62u) + (jump ? 2u : 0u);
-}
-
 // Order-preserving key of a score; -0 ranks with +0 and NaN below everything.
 __device__ __forceinline__ uint32_t score_okey(float x) {
     x = __fadd_rn(x, 0.0f);
