@@ -144,114 +144,96 @@ __global__ void prep_elites_kernel(const csx_genome *__restrict__ el, int ne, fl
 
 // ---- 1. walk ------------------------------------------------------------------
 
-// Group-speculative walking. G lanes evaluate the next G candidate starts of
-// one chain assuming every step is the common 62-draw one (no immigrant, no
-// jump): lane j tests the candidate at x + 62 j. A ballot finds the first lane
-// whose tests say otherwise (f); candidates x + 62 i for i <= f are then the
-// chain's true next starts, and lane f's tests give its step length. The chain
-// advances about min(G, 33) candidates per round at the latency of one hash.
-struct Round {
-    uint32_t f;    // first lane with a non-62 step, G if none
-    uint32_t len;  // that step's length (33/35/64); 62 when f == G
+// One thread per segment: the segment's guess chain from its first draw to
+// its first start at or past the segment end, a checkpoint every D starts.
+__global__ void walk_kernel(SynthConst sc, StreamGeom g, SegRec *__restrict__ recs,
+                            uint64_t *__restrict__ ck, Ctrl *__restrict__ ctrl) {
+    const uint64_t s = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (s >= g.n_seg) return;
+    uint64_t t;
+    uint32_t c;
+    seg_of(g, s, t, c);
+    const bool last_stream = t == g.T - 1;
+    const uint64_t my = last_stream ? g.my_last : g.per;
+    const uint32_t ct = last_stream ? g.C_last : g.C;
+    const uint64_t seed_t = stream_seed(g.seed, t);
+    const uint64_t b = static_cast<uint64_t>(c) * g.L, e = b + g.L;
+    uint64_t *ckp = ck + s * g.ckcap;
+    const uint64_t dmask = (1ull << g.d_log2) - 1;
+    uint64_t p = b, k = 0;
+    const uint64_t limit = (ct == 1) ? my : ~0ull;  // a lone segment starts at the truth
+    while (p < e && k < limit) {
+        if ((k & dmask) == 0) {
+            const uint64_t m = k >> g.d_log2;
+            if (m < g.ckcap) ckp[m] = p;
+        }
+        p = walk_step2(sc, seed_t, p);
+        ++k;
+    }
+    SegRec r;
+    r.n = static_cast<uint32_t>(k);
+    r.a = 0;
+    r.b_next = 0;
+    r.merge_pos = p;  // the chain's first start at or past the segment end
+    r.status = (c + 1 == ct) ? kSegLast : kSegOk;
+    recs[s] = r;
+}
+
+// Speculative run of one chain by a half-warp: lane j tests the start x + 62 j
+// assuming every earlier step of the run is the common 62-draw one (no
+// immigrant, no jump). f = first lane whose tests say otherwise (16 if none);
+// the run's starts are x + 62 i for i <= min(f, 15) and the next start after
+// it is x + 62 f + len (or x + 62*16).
+struct Run {
+    uint32_t n;     // starts in the run
+    uint64_t next;  // the chain's next start after the run
 };
 
-template <int G>
-__device__ __forceinline__ Round walk_round(const SynthConst &C, uint64_t seed_t, uint64_t x, int j,
-                                            int gbase) {
+__device__ __forceinline__ Run half_run(const SynthConst &C, uint64_t seed_t, uint64_t x, int j, int half) {
     const uint64_t pj = x + 62ull * static_cast<uint64_t>(j);
-    const uint64_t s0 = seed_t + (pj + 1) * kGolden;              // state of draw pj
+    const uint64_t s0 = seed_t + (pj + 1) * kGolden;               // state of draw pj
     const bool imm = (draw_vh(s0 + 2 * kGolden) >> 8) < C.imm_thr;  // draw pj + 2
     const bool jb = (draw_vh(s0 + 61 * kGolden) >> 8) < C.jump_thr; // draw pj + 61
-    const uint32_t gmask = (G == 32) ? 0xffffffffu : ((1u << G) - 1u);
-    const uint32_t bn = (__ballot_sync(0xffffffffu, imm || jb) >> gbase) & gmask;
-    const uint32_t bi = (__ballot_sync(0xffffffffu, imm) >> gbase) & gmask;
-    Round r;
-    r.f = bn ? static_cast<uint32_t>(__ffs(bn) - 1) : static_cast<uint32_t>(G);
-    r.len = 62;
-    if (r.f < static_cast<uint32_t>(G)) {
-        if ((bi >> r.f) & 1u) {  // immigrant: its jump test is at draw + 32
-            const uint64_t pf = x + 62ull * r.f;
-            const bool ja = (draw_vh(seed_t + (pf + 33) * kGolden) >> 8) < C.jump_thr;
-            r.len = ja ? 35 : 33;
-        } else {
-            r.len = 64;  // a jump after a crossover candidate
-        }
+    const uint32_t bn = (__ballot_sync(0xffffffffu, imm || jb) >> (16 * half)) & 0xffffu;
+    const uint32_t bi = (__ballot_sync(0xffffffffu, imm) >> (16 * half)) & 0xffffu;
+    Run r;
+    if (bn == 0) {
+        r.n = 16;
+        r.next = x + 62ull * 16;
+        return r;
     }
+    const uint32_t f = static_cast<uint32_t>(__ffs(bn) - 1);
+    const uint64_t pf = x + 62ull * f;
+    uint32_t len = 64;            // a jump after a crossover candidate
+    if ((bi >> f) & 1u) {         // an immigrant: its jump test is at draw + 32
+        const bool ja = (draw_vh(seed_t + (pf + 33) * kGolden) >> 8) < C.jump_thr;
+        len = ja ? 35 : 33;
+    }
+    r.n = f + 1;
+    r.next = pf + len;
     return r;
 }
 
-// Record the checkpoint (start of every D-th candidate) falling in the
-// candidates [k, k + cnt) whose starts are x + 62 (idx - k); D >= 64 > cnt,
-// so at most one per round.
+// Checkpoint (start of every D-th candidate) among the starts [k, k + cnt),
+// which lie at x + 62 (idx - k); D >= 64 > cnt, so at most one.
 __device__ __forceinline__ void record_ckpt(uint64_t *ckp, uint32_t ckcap, uint32_t dl, uint64_t k,
                                             uint64_t cnt, uint64_t x) {
     const uint64_t mk = ((k + (1ull << dl) - 1) >> dl) << dl;
     if (mk < k + cnt && (mk >> dl) < ckcap) ckp[mk >> dl] = x + 62ull * (mk - k);
 }
 
-constexpr int kWalkGroup = 8;   // lanes per segment walk
-constexpr int kLinkGroup = 32;  // lanes per link
-
-// One group of kWalkGroup lanes per segment: the segment's guess chain from
-// its first draw to its first start at or past the segment end.
-__global__ void walk_kernel(SynthConst sc, StreamGeom g, SegRec *__restrict__ recs,
-                            uint64_t *__restrict__ ck, Ctrl *__restrict__ ctrl) {
-    constexpr int G = kWalkGroup;
-    const int lane = threadIdx.x & 31, gbase = lane & ~(G - 1), j = lane & (G - 1);
-    const uint64_t s = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) / G;
-    const bool valid = s < g.n_seg;
-    uint64_t t = 0;
-    uint32_t c = 0;
-    if (valid) seg_of(g, s, t, c);
-    const bool last_stream = t == g.T - 1;
-    const uint64_t my = last_stream ? g.my_last : g.per;
-    const uint32_t ct = last_stream ? g.C_last : g.C;
-    const uint64_t seed_t = stream_seed(g.seed, t);
-    const uint64_t b = static_cast<uint64_t>(c) * g.L, e = b + g.L;
-    uint64_t *ckp = ck + (valid ? s : 0) * g.ckcap;
-    const uint64_t limit = (ct == 1) ? my : ~0ull;  // a lone segment starts at the truth
-    uint64_t p = b, k = 0;
-    bool going = valid && p < e && k < limit;
-    while (__any_sync(0xffffffffu, going)) {
-        const Round r = walk_round<G>(sc, seed_t, p, j, gbase);
-        if (going) {
-            const uint64_t i_e = (e - p + 61) / 62;  // candidates whose start stays below e
-            const uint64_t i_cap = i_e < limit - k ? i_e : limit - k;
-            uint64_t cnt, np;
-            if (r.f < i_cap && r.f < static_cast<uint32_t>(G)) {
-                cnt = r.f + 1;
-                np = p + 62ull * r.f + r.len;
-            } else {
-                cnt = i_cap < static_cast<uint64_t>(G) ? i_cap : static_cast<uint64_t>(G);
-                np = p + 62ull * cnt;
-            }
-            if (j == 0) record_ckpt(ckp, g.ckcap, g.d_log2, k, cnt, p);
-            p = np;
-            k += cnt;
-            going = p < e && k < limit;
-        }
-    }
-    if (valid && j == 0) {
-        SegRec rec;
-        rec.n = static_cast<uint32_t>(k);
-        rec.a = 0;
-        rec.b_next = 0;
-        rec.merge_pos = p;  // the chain's first start at or past the segment end
-        rec.status = (c + 1 == ct) ? kSegLast : kSegOk;
-        recs[s] = rec;
-    }
-}
-
 // One warp per link of segment s and s+1 (same stream): s's chain from its
-// exit and s+1's guess chain from its first draw, advancing whichever is
-// behind by speculative rounds that never pass the leader unchecked, until
-// they share a start.
+// exit (lanes 0-15) and s+1's guess chain from its first draw (lanes 16-31)
+// advance together in speculative runs. Below M = the nearer of the two next
+// starts both chains' starts are known, and within a run they are 62 apart,
+// so the first shared start below M is y if (y - x) is a multiple of 62
+// inside x's run (or symmetrically). Otherwise both move to their first start
+// at or past M and the search goes on.
 __global__ void link_kernel(SynthConst sc, StreamGeom g, SegRec *__restrict__ recs,
                             uint64_t *__restrict__ ck, Ctrl *__restrict__ ctrl) {
-    constexpr int G = kLinkGroup;
-    const int lane = threadIdx.x & 31, gbase = lane & ~(G - 1), j = lane & (G - 1);
-    const uint64_t s = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) / G;
-    if (s >= g.n_seg) return;  // whole groups leave together
+    const int lane = threadIdx.x & 31, half = lane >> 4, j = lane & 15;
+    const uint64_t s = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    if (s >= g.n_seg) return;  // whole warps leave together
     SegRec r = recs[s];
     if (r.status != kSegOk) return;
     uint64_t t;
@@ -259,43 +241,57 @@ __global__ void link_kernel(SynthConst sc, StreamGeom g, SegRec *__restrict__ re
     seg_of(g, s, t, c);
     const uint64_t seed_t = stream_seed(g.seed, t);
     uint64_t *ckp = ck + s * g.ckcap;
-    uint64_t p = r.merge_pos, k = r.n;                        // chain of segment s
-    uint64_t q = static_cast<uint64_t>(c + 1) * g.L, kb = 0;  // guess chain of s + 1
+    uint64_t x = r.merge_pos, k = r.n;                        // chain of segment s
+    uint64_t y = static_cast<uint64_t>(c + 1) * g.L, kb = 0;  // guess chain of s + 1
     uint64_t steps = 0;
     bool fail = false;
-    while (p != q) {
-        const bool a = p < q;  // advance the chain that is behind
-        const uint64_t x = a ? p : q, y = a ? q : p;
-        const Round rd = walk_round<G>(sc, seed_t, x, j, gbase);
-        const uint64_t i_y = (y - x + 61) / 62;  // 62-steps to reach y or beyond
-        uint64_t cnt, nx;
-        if (rd.f < i_y && rd.f < static_cast<uint32_t>(G)) {
-            cnt = rd.f + 1;
-            nx = x + 62ull * rd.f + rd.len;
+    while (x != y) {
+        const Run mine = half_run(sc, seed_t, half ? y : x, j, half);
+        Run rx, ry;
+        rx.n = __shfl_sync(0xffffffffu, mine.n, 0);
+        rx.next = __shfl_sync(0xffffffffu, mine.next, 0);
+        ry.n = __shfl_sync(0xffffffffu, mine.n, 16);
+        ry.next = __shfl_sync(0xffffffffu, mine.next, 16);
+        const uint64_t m = rx.next < ry.next ? rx.next : ry.next;
+        // starts below m: x + 62 i for i < ix, y + 62 i for i < iy
+        const uint64_t ix = m > x ? std::min<uint64_t>(rx.n, (m - x + 61) / 62) : 0;
+        const uint64_t iy = m > y ? std::min<uint64_t>(ry.n, (m - y + 61) / 62) : 0;
+        bool met = false;
+        uint64_t adv_x = ix, adv_y = iy;
+        if (x < y) {
+            const uint64_t d = y - x;
+            if (d % 62 == 0 && d / 62 < ix) {  // y is one of x's starts below m
+                met = true;
+                adv_x = d / 62;
+                adv_y = 0;
+            }
         } else {
-            cnt = i_y < static_cast<uint64_t>(G) ? i_y : static_cast<uint64_t>(G);
-            nx = x + 62ull * cnt;
+            const uint64_t d = x - y;
+            if (d % 62 == 0 && d / 62 < iy) {
+                met = true;
+                adv_x = 0;
+                adv_y = d / 62;
+            }
         }
-        if (a) {
-            if (j == 0) record_ckpt(ckp, g.ckcap, g.d_log2, k, cnt, x);
-            p = nx;
-            k += cnt;
-        } else {
-            q = nx;
-            kb += cnt;
-        }
-        steps += cnt;
+        if (lane == 0) record_ckpt(ckp, g.ckcap, g.d_log2, k, adv_x, x);
+        const uint64_t nx = met ? x + 62ull * adv_x : (ix == rx.n ? rx.next : x + 62ull * ix);
+        const uint64_t ny = met ? y + 62ull * adv_y : (iy == ry.n ? ry.next : y + 62ull * iy);
+        k += adv_x;
+        kb += adv_y;
+        x = nx;
+        y = ny;
+        steps += adv_x + adv_y;
         if (steps > kLinkCap) {
             fail = true;
             break;
         }
     }
-    if (j == 0) {
+    if (lane == 0) {
         if (fail) {
             r.status = kSegFail;
             atomicOr(&ctrl->err, kErrLink);
         }
-        r.merge_pos = p;
+        r.merge_pos = x;
         r.a = static_cast<uint32_t>(k - r.n);
         r.b_next = static_cast<uint32_t>(kb);
         recs[s] = r;
@@ -1055,9 +1051,9 @@ int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, cons
         auto *ck = static_cast<uint64_t *>(cx.ck.p);
         auto *so = static_cast<SegOut *>(cx.segout.p);
         auto *off = static_cast<uint32_t *>(cx.off.p);
-        walk_kernel<<<unit_blocks(g.n_seg * kWalkGroup, 128), 128, 0, st>>>(sc, g, recs, ck, ctrl);
+        walk_kernel<<<unit_blocks(g.n_seg, 128), 128, 0, st>>>(sc, g, recs, ck, ctrl);
         CSX_CUDA(cudaGetLastError());
-        link_kernel<<<unit_blocks(g.n_seg * kLinkGroup, 128), 128, 0, st>>>(sc, g, recs, ck, ctrl);
+        link_kernel<<<unit_blocks(g.n_seg * 32, 128), 128, 0, st>>>(sc, g, recs, ck, ctrl);
         CSX_CUDA(cudaGetLastError());
         if (g.C >= 64)
             assemble_block_kernel<<<static_cast<unsigned>(g.T), kAsmThreads, 0, st>>>(g, recs, so, ctrl);
@@ -1410,9 +1406,9 @@ int enqueue_screen_noalloc(const NoAllocDevice &dv, const csx_cfg &cfg, const cs
         stream_items_kernel<<<unit_blocks(g.T, 256), 256, 0, st>>>(g, items, ctrl);
         CSX_CUDA(cudaGetLastError());
     } else {
-        walk_kernel<<<unit_blocks(g.n_seg * kWalkGroup, 128), 128, 0, st>>>(sc, g, recs, ck, ctrl);
+        walk_kernel<<<unit_blocks(g.n_seg, 128), 128, 0, st>>>(sc, g, recs, ck, ctrl);
         CSX_CUDA(cudaGetLastError());
-        link_kernel<<<unit_blocks(g.n_seg * kLinkGroup, 128), 128, 0, st>>>(sc, g, recs, ck, ctrl);
+        link_kernel<<<unit_blocks(g.n_seg * 32, 128), 128, 0, st>>>(sc, g, recs, ck, ctrl);
         CSX_CUDA(cudaGetLastError());
         if (g.C >= 64)
             assemble_block_kernel<<<static_cast<unsigned>(g.T), kAsmThreads, 0, st>>>(g, recs, so, ctrl);
