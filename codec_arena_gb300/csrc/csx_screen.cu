@@ -342,10 +342,13 @@ __global__ void assemble_kernel(StreamGeom g, const SegRec *__restrict__ recs, S
     if (idx != my) atomicOr(&ctrl->err, kErrAssemble);
 }
 
-// One CTA per stream. Segment c's truth range starts where link c-1 met
-// (lo = b_next of c-1, pos = its merge_pos) unless that meeting lies before
-// the truth reached chain c-1 (lo > hi there); the block checks every segment
-// for that case and, if it occurs (rare), falls back to the sequential loop.
+// One CTA per stream, 256 segments per tile. Segment c's truth range starts
+// where link c-1 met (lo = b_next of c-1, pos = its merge_pos) unless segment
+// c-1 was late: the truth reached c-1's chain only after that chain had met
+// c's (lo > hi at c-1); then c's start is carried over (lo = b_next of c-1 +
+// lo - hi of c-1, same pos). Late segments are rare and isolated, so the
+// block computes the common case in parallel and thread 0 repairs the short
+// runs after each late segment, carrying a pending state into the next tile.
 constexpr int kAsmThreads = 256;
 
 __global__ void __launch_bounds__(kAsmThreads) assemble_block_kernel(StreamGeom g,
@@ -353,8 +356,11 @@ __global__ void __launch_bounds__(kAsmThreads) assemble_block_kernel(StreamGeom 
                                                                       SegOut *__restrict__ outs,
                                                                       Ctrl *__restrict__ ctrl) {
     __shared__ unsigned long long wsum[kAsmThreads / 32];
+    __shared__ uint64_t s_lo[kAsmThreads], s_pos[kAsmThreads], s_hi[kAsmThreads];
+    __shared__ uint32_t s_late[kAsmThreads / 32];
     __shared__ unsigned long long carry;
-    __shared__ int irregular;
+    __shared__ int pending, failed;
+    __shared__ uint64_t pend_lo, pend_pos;
     const uint64_t t = blockIdx.x;
     const bool last_stream = t == g.T - 1;
     const uint64_t my = last_stream ? g.my_last : g.per;
@@ -363,28 +369,79 @@ __global__ void __launch_bounds__(kAsmThreads) assemble_block_kernel(StreamGeom 
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     if (tid == 0) {
         carry = 0;
-        irregular = 0;
+        pending = 0;
+        failed = 0;
     }
     __syncthreads();
     for (uint32_t base = 0; base < ct; base += kAsmThreads) {
         const uint32_t c = base + tid;
-        uint64_t lo = 0, pos = 0, len = 0, hi = 0;
-        bool bad = false;
+        bool late = false, bad = false;
         if (c < ct) {
             const SegRec r = recs[s0 + c];
+            uint64_t lo = 0, pos = 0;
             if (c > 0) {
                 const SegRec q = recs[s0 + c - 1];
                 lo = q.b_next;
                 pos = q.merge_pos;
                 bad |= q.status == kSegFail;
             }
-            hi = (r.status == kSegLast) ? r.n : static_cast<uint64_t>(r.n) + r.a;
-            bad |= r.status == kSegFail || lo > hi;
-            len = hi > lo ? hi - lo : 0;
+            const uint64_t hi = (r.status == kSegLast) ? r.n : static_cast<uint64_t>(r.n) + r.a;
+            bad |= r.status == kSegFail;
+            late = lo > hi;
+            s_lo[tid] = lo;
+            s_pos[tid] = pos;
+            s_hi[tid] = hi;
         }
-        if (__syncthreads_or(bad)) {
-            if (tid == 0) irregular = 1;
-            break;
+        const uint32_t lb = __ballot_sync(0xffffffffu, late);
+        if (lane == 0) s_late[w] = lb;
+        if (__syncthreads_or(bad) && tid == 0) failed = 1;
+        if (tid == 0) {  // repair the runs that follow late segments, in order
+            const uint32_t n_here = min(static_cast<uint32_t>(kAsmThreads), ct - base);
+            constexpr uint32_t kNone = 0xffffffffu;
+            uint32_t x = kNone, from = 0;
+            if (pending) {  // the previous tile ended inside a run
+                s_lo[0] = pend_lo;
+                s_pos[0] = pend_pos;
+                pending = 0;
+                x = 0;
+            }
+            for (;;) {
+                if (x == kNone) {  // next flagged segment at or after `from`
+                    for (uint32_t q = from >> 5; q < kAsmThreads / 32 && x == kNone; ++q) {
+                        uint32_t bits = s_late[q];
+                        if (q == (from >> 5)) bits &= ~((1u << (from & 31)) - 1u);
+                        if (bits) x = q * 32 + __ffs(bits) - 1;
+                    }
+                    if (x == kNone || x >= n_here) break;
+                }
+                // x's state is its true one; carry while it is late
+                while (s_lo[x] > s_hi[x]) {
+                    const SegRec r = recs[s0 + base + x];
+                    const uint64_t nlo = static_cast<uint64_t>(r.b_next) + (s_lo[x] - s_hi[x]);
+                    if (x + 1 < n_here) {
+                        s_lo[x + 1] = nlo;
+                        s_pos[x + 1] = s_pos[x];
+                        ++x;
+                    } else {
+                        if (base + x + 1 < ct) {
+                            pending = 1;
+                            pend_lo = nlo;
+                            pend_pos = s_pos[x];
+                        }
+                        break;
+                    }
+                }
+                from = x + 1;
+                x = kNone;
+                if (from >= n_here) break;
+            }
+        }
+        __syncthreads();
+        uint64_t lo = 0, pos = 0, len = 0;
+        if (c < ct) {
+            lo = s_lo[tid];
+            pos = s_pos[tid];
+            len = s_hi[tid] > lo ? s_hi[tid] - lo : 0;
         }
         // block exclusive scan of len
         unsigned long long v = len;
@@ -411,7 +468,7 @@ __global__ void __launch_bounds__(kAsmThreads) assemble_block_kernel(StreamGeom 
             o.lo = lo;
             o.cnt = 0;
             o.nitems = 0;
-            if (idx < my && len > 0) {
+            if (!failed && idx < my && len > 0) {
                 const uint64_t cnt = len < my - idx ? len : my - idx;
                 uint64_t mmin, mmax;
                 split_range(lo, cnt, g.d_log2, g.ckcap, mmin, mmax);
@@ -424,45 +481,7 @@ __global__ void __launch_bounds__(kAsmThreads) assemble_block_kernel(StreamGeom 
         if (tid == kAsmThreads - 1) carry += wsum[kAsmThreads / 32 - 1];
         __syncthreads();
     }
-    __syncthreads();
-    if (irregular) {
-        if (tid == 0) {  // sequential: follows the truth through late meetings
-            uint64_t lo = 0, pos = 0, idx = 0;
-            bool bad = false;
-            for (uint32_t c = 0; c < ct; ++c) {
-                const SegRec r = recs[s0 + c];
-                SegOut o;
-                o.pos = pos;
-                o.I = idx;
-                o.lo = lo;
-                o.cnt = 0;
-                o.nitems = 0;
-                if (r.status == kSegFail) bad = true;
-                const uint64_t hi = (r.status == kSegLast) ? r.n : static_cast<uint64_t>(r.n) + r.a;
-                if (!bad && idx < my && hi > lo) {
-                    uint64_t cnt = hi - lo;
-                    if (cnt > my - idx) cnt = my - idx;
-                    uint64_t mmin, mmax;
-                    split_range(lo, cnt, g.d_log2, g.ckcap, mmin, mmax);
-                    o.cnt = static_cast<uint32_t>(cnt);
-                    o.nitems = 1 + (mmax >= mmin ? static_cast<uint32_t>(mmax - mmin + 1) : 0u);
-                    idx += cnt;
-                }
-                outs[s0 + c] = o;
-                if (r.status == kSegOk) {
-                    if (hi >= lo) {
-                        lo = r.b_next;
-                        pos = r.merge_pos;
-                    } else {
-                        lo = r.b_next + (lo - hi);
-                    }
-                }
-            }
-            if (idx != my) atomicOr(&ctrl->err, kErrAssemble);
-        }
-    } else if (tid == 0 && carry < my) {
-        atomicOr(&ctrl->err, kErrAssemble);
-    }
+    if (tid == 0 && (failed || carry < my)) atomicOr(&ctrl->err, kErrAssemble);
 }
 
 // ---- 3. scan + emit ---------------------------------------------------------------

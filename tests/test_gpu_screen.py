@@ -317,3 +317,16 @@ def test_filter_near_ties(orc):
     el["g"][:] = np.where(el["g"] > 0.5, 2.0, -1.0)
     got = check(orc, 100_000, 200, 3, 4, w, el, sigma=0.1, imm=0.0, jump=0.0, ties="aware")
     assert len(np.unique(got["score"])) < len(got)  # the case really has ties
+
+
+def test_late_meetings_block_assembly(orc, env):
+    """Segments of 2000 candidates are shorter than a typical meeting of two
+    chains (~3.3k candidates per chain), so many segments are late: their
+    incoming meeting lies past their outgoing one. The block assembly repairs
+    those runs locally; the survivors must still equal the oracle's."""
+    from codec_arena_gb300 import workloads as wl
+
+    env.setenv("CSX_SEG_CANDS", "2000")
+    check(orc, 20_000_000, 128, 23, 4, wl.surrogate_161(), wl.seeded_elites(64))
+    env.setenv("CSX_SEG_CANDS", "700")
+    check(orc, 6_000_000, 64, 5, 3, wl.seeded_normal_model(), wl.seeded_elites(20), imm=0.05, jump=0.1)
