@@ -253,24 +253,24 @@ __global__ void link_kernel(SynthConst sc, StreamGeom g, SegRec *__restrict__ re
         ry.n = __shfl_sync(0xffffffffu, mine.n, 16);
         ry.next = __shfl_sync(0xffffffffu, mine.next, 16);
         const uint64_t m = rx.next < ry.next ? rx.next : ry.next;
-        // starts below m: x + 62 i for i < ix, y + 62 i for i < iy
-        const uint64_t ix = m > x ? std::min<uint64_t>(rx.n, (m - x + 61) / 62) : 0;
-        const uint64_t iy = m > y ? std::min<uint64_t>(ry.n, (m - y + 61) / 62) : 0;
+        // starts below m: x + 62 i for i < ix, y + 62 i for i < iy. Both chains
+        // lie within a run (< 17 * 64 draws) of each other and of m, so the
+        // differences fit 32 bits.
+        const uint32_t ix = m > x ? min(rx.n, (static_cast<uint32_t>(m - x) + 61u) / 62u) : 0u;
+        const uint32_t iy = m > y ? min(ry.n, (static_cast<uint32_t>(m - y) + 61u) / 62u) : 0u;
         bool met = false;
-        uint64_t adv_x = ix, adv_y = iy;
-        if (x < y) {
-            const uint64_t d = y - x;
-            if (d % 62 == 0 && d / 62 < ix) {  // y is one of x's starts below m
+        uint32_t adv_x = ix, adv_y = iy;
+        const uint32_t d = static_cast<uint32_t>(x < y ? y - x : x - y);
+        const uint32_t dq = d / 62u;
+        if (dq * 62u == d) {  // the leading start is on the lagging chain's run?
+            if (x < y && dq < ix) {
                 met = true;
-                adv_x = d / 62;
+                adv_x = dq;
                 adv_y = 0;
-            }
-        } else {
-            const uint64_t d = x - y;
-            if (d % 62 == 0 && d / 62 < iy) {
+            } else if (x > y && dq < iy) {
                 met = true;
                 adv_x = 0;
-                adv_y = d / 62;
+                adv_y = dq;
             }
         }
         if (lane == 0) record_ckpt(ckp, g.ckcap, g.d_log2, k, adv_x, x);
@@ -624,7 +624,7 @@ __device__ __noinline__ float exact_score_at(const ScreenArgs *__restrict__ A, c
 // kFilter: score with the FFMA filter form and evaluate the reference's f32
 // order only when the filter score is within A.err of the threshold.
 template <bool kFastDelta, bool kFilter>
-__global__ void __launch_bounds__(kThreads) screen_kernel(const __grid_constant__ ScreenArgs A) {
+__global__ void __launch_bounds__(kThreads, 3) screen_kernel(const __grid_constant__ ScreenArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Entry *E = reinterpret_cast<Entry *>(smem_raw);
     float *el = reinterpret_cast<float *>(E + A.sort_n);
