@@ -43,7 +43,7 @@
 namespace csx {
 
 constexpr int kThreads = 256;      // screen CTA
-constexpr int kRounds = 2;         // candidates per thread between buffer checks
+constexpr int kRounds = 8;         // candidates per thread between CTA barriers
 constexpr uint32_t kMaxKeep = 4096;
 constexpr uint32_t kMaxElites = 1536;
 constexpr uint64_t kLinkCap = 1ull << 26;
@@ -659,12 +659,17 @@ __global__ void __launch_bounds__(kThreads, 3) screen_kernel(const __grid_consta
     unsigned long long screened = 0, exact = 0;
     unsigned int gk = 0;
     uint32_t round = 0;
+    // An append that finds the buffer full is held here and the thread pauses
+    // until the next merge (which the full buffer forces), so no entry is lost
+    // and the buffer never needs room for a whole round of appends.
+    bool has_def = false;
+    Entry def{0ull, 0ull};
 
     for (;;) {
         __syncthreads();
         const unsigned int bn = s_buf_n;  // nobody appends until after the next barrier
-        const int any = __syncthreads_or(valid);
-        if (bn > A.buf_cap - kRounds * kThreads || (!any && bn > 0)) {
+        const int any = __syncthreads_or(valid || has_def);
+        if (bn >= A.buf_cap / 2 || (!any && bn > 0)) {
             cta_sort_desc(E, A.sort_n);
             for (uint32_t i = A.kpad + tid; i < A.sort_n; i += kThreads) E[i] = Entry{0ull, 0ull};
             if (tid == 0) {
@@ -681,6 +686,11 @@ __global__ void __launch_bounds__(kThreads, 3) screen_kernel(const __grid_consta
             __syncthreads();
         }
         if (!any) break;
+        if (has_def) {  // the merge above emptied the buffer: room for every held entry
+            const unsigned int slot = atomicAdd(&s_buf_n, 1u);
+            buf[slot] = def;
+            has_def = false;
+        }
         unsigned long long t1 = s_t1, t2 = s_t2;
         float ts = s_ts;
         if ((round++ & 7u) == 0) gk = *reinterpret_cast<volatile unsigned int *>(&A.ctrl->gtau);
@@ -691,7 +701,7 @@ __global__ void __launch_bounds__(kThreads, 3) screen_kernel(const __grid_consta
         }
         const float tlo = kFilter ? __fsub_rd(ts, A.err) : ts;
 #pragma unroll 1
-        for (int r = 0; r < kRounds && valid; ++r) {
+        for (int r = 0; r < kRounds && valid && !has_def; ++r) {
             const CandHead h = cand_head(A.sc, seed_t, p);
             float s;
             if (kFilter) {
@@ -712,7 +722,12 @@ __global__ void __launch_bounds__(kThreads, 3) screen_kernel(const __grid_consta
                     (static_cast<unsigned long long>(~dcand) << 32) | ddraw;
                 if (k1 > t1 || (k1 == t1 && k2 > t2)) {
                     const unsigned int slot = atomicAdd(&s_buf_n, 1u);
-                    buf[slot] = Entry{k1, k2};
+                    if (slot < A.buf_cap) {
+                        buf[slot] = Entry{k1, k2};
+                    } else {
+                        has_def = true;
+                        def = Entry{k1, k2};
+                    }
                 }
             }
             p += h.len;
@@ -965,7 +980,7 @@ int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int
     pl->filter = !(cfg.flags & CSX_FLAG_EXACT_ALL) && pl->err > 0.0f;
 
     pl->kpad = std::max<uint32_t>(32, pow2_at_least(cfg.keep));
-    pl->sort_n = pow2_at_least(pl->kpad + 2ull * kRounds * kThreads);
+    pl->sort_n = pow2_at_least(pl->kpad + 4ull * kThreads);
     pl->buf_cap = pl->sort_n - pl->kpad;
     pl->smem = static_cast<size_t>(pl->sort_n) * sizeof(Entry) +
                static_cast<size_t>(ne + 1) * kNtot * sizeof(float);
@@ -1331,7 +1346,7 @@ int plan_noalloc(const NoAllocDevice &dv, const csx_cfg &cfg, const csx_model &m
     pl->err = filter_bound(model);
     pl->filter = !(cfg.flags & CSX_FLAG_EXACT_ALL) && pl->err > 0.0f;
     pl->kpad = std::max<uint32_t>(32, pow2_at_least(cfg.keep));
-    pl->sort_n = pow2_at_least(pl->kpad + 2ull * kRounds * kThreads);
+    pl->sort_n = pow2_at_least(pl->kpad + 4ull * kThreads);
     pl->buf_cap = pl->sort_n - pl->kpad;
     pl->smem = static_cast<size_t>(pl->sort_n) * sizeof(Entry) +
                static_cast<size_t>(ne + 1) * kNtot * sizeof(float);
