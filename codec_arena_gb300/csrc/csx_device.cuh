@@ -41,8 +41,8 @@ struct SynthConst {
     uint32_t imm_thr;   // unit() < imm_p   <=>  (next() >> 40) < imm_thr
     uint32_t jump_thr;  // unit() < jump_p  <=>  (next() >> 40) < jump_thr
     float sigma;
-    float nsig1;  // -sigma
-    float nsig2;  // -2 sigma
+    float nsig1;    // -sigma
+    float sigma23;  // sigma * 2^-23 (exact in the fast delta form)
 };
 
 __host__ __device__ constexpr int tri(int i, int j) { return i * (i + 1) / 2 + j; }
@@ -118,10 +118,12 @@ __device__ __forceinline__ CandHead cand_head(const SynthConst &C, uint64_t seed
 // parents on a row of 0.5s and half-width 0.5: 0.5 + (u - 0.5) == u exactly.
 // Their unit draws are consecutive; crossover genes alternate bit and unit.
 //
-// kFastDelta: delta = fma(y, B, -c*B) with y in [1,2), c in {1,2}; -c*B is
-// exact, so this is one rounding of (y-c)*B == round((u-0.5)*2*B). Valid for
-// finite |B| <= 1e38 (then |delta| < |B| is finite too); otherwise the
-// two-op form is used.
+// kFastDelta: (u - 0.5) * 2 = k * 2^-23 - 1 with k = next() >> 40, so the
+// mutation round((u - 0.5) * 2 * B) is one FFMA, fma(float(k), B * 2^-23, -B):
+// float(k) (24 bits), B * 2^-23 and -B are exact and the FFMA rounds once.
+// Valid for B = 0 or 1e-30 <= |B| <= 1e38 (B * 2^-23 stays normal, |delta|
+// < |B| stays finite); otherwise the two-op form builds u - 0.5 exactly from
+// the mantissa bits and multiplies.
 //
 // kExact = false computes a filter score instead: the same surface by FFMA
 // Horner, t_l = w_l + sum_{i>=l} Wq[i][l] g_i, s = 16 w0 + sum_l g_l t_l +
@@ -139,7 +141,7 @@ __device__ __forceinline__ float synth_score(const DevModel &M, const SynthConst
     const float *pb = el + rb * kNtot;
     const float B = h.imm ? 0.5f : C.sigma;
     const float nb1 = h.imm ? -0.5f : C.nsig1;
-    const float nb2 = h.imm ? -1.0f : C.nsig2;
+    const float B23 = h.imm ? 0x1p-24f : C.sigma23;
     const uint64_t step = h.imm ? kGolden : 2 * kGolden;
     uint64_t su = s0 + (h.imm ? 3ull : 4ull) * kGolden;  // unit draw of gene 0
 
@@ -152,12 +154,11 @@ __device__ __forceinline__ float synth_score(const DevModel &M, const SynthConst
         su += step;
         const float *src = (static_cast<int32_t>(bw) < 0) ? pb : pa;
         const float par = src[k];
-        const float y = __uint_as_float(((vh >> 8) & 0x7FFFFFu) | 0x3F800000u);
         float g;
         if (kFastDelta) {
-            const float nc = (static_cast<int32_t>(vh) < 0) ? nb1 : nb2;
-            g = __fadd_rn(par, __fmaf_rn(y, B, nc));
+            g = __fadd_rn(par, __fmaf_rn(__uint2float_rn(vh >> 8), B23, nb1));
         } else {
+            const float y = __uint_as_float(((vh >> 8) & 0x7FFFFFu) | 0x3F800000u);
             const float nc = (static_cast<int32_t>(vh) < 0) ? -1.0f : -2.0f;
             g = __fadd_rn(par, __fmul_rn(__fadd_rn(y, nc), B));
         }

@@ -975,7 +975,8 @@ int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int
     g.my_last = cfg.lambda - (g.T - 1) * g.per;
     const uint64_t my_max = std::max(g.per, g.my_last);
     if (g.T >= 0xFFFFFFFFull) return CSX_ERR_LIMIT;
-    pl->fast_delta = std::isfinite(cfg.sigma) && std::fabs(cfg.sigma) <= 1.0e38f;
+    pl->fast_delta = std::isfinite(cfg.sigma) && std::fabs(cfg.sigma) <= 1.0e38f &&
+                     (cfg.sigma == 0.0f || std::fabs(cfg.sigma) >= 1.0e-30f);
     pl->err = filter_bound(model);
     pl->filter = !(cfg.flags & CSX_FLAG_EXACT_ALL) && pl->err > 0.0f;
 
@@ -1064,7 +1065,7 @@ int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, cons
     sc.jump_thr = unit_threshold(cfg.jump_p);
     sc.sigma = cfg.sigma;
     sc.nsig1 = -cfg.sigma;
-    sc.nsig2 = -2.0f * cfg.sigma;
+    sc.sigma23 = cfg.sigma * 0x1p-23f;
 
     float *tab = static_cast<float *>(cx.tab.p);
     auto *ids = static_cast<unsigned long long *>(cx.ids.p);
@@ -1342,7 +1343,8 @@ int plan_noalloc(const NoAllocDevice &dv, const csx_cfg &cfg, const csx_model &m
     g.my_last = cfg.lambda - (g.T - 1) * g.per;
     const uint64_t my_max = std::max(g.per, g.my_last);
     if (g.T >= 0xFFFFFFFFull) return CSX_ERR_LIMIT;
-    pl->fast_delta = std::isfinite(cfg.sigma) && std::fabs(cfg.sigma) <= 1.0e38f;
+    pl->fast_delta = std::isfinite(cfg.sigma) && std::fabs(cfg.sigma) <= 1.0e38f &&
+                     (cfg.sigma == 0.0f || std::fabs(cfg.sigma) >= 1.0e-30f);
     pl->err = filter_bound(model);
     pl->filter = !(cfg.flags & CSX_FLAG_EXACT_ALL) && pl->err > 0.0f;
     pl->kpad = std::max<uint32_t>(32, pow2_at_least(cfg.keep));
@@ -1432,7 +1434,7 @@ int enqueue_screen_noalloc(const NoAllocDevice &dv, const csx_cfg &cfg, const cs
     sc.jump_thr = unit_threshold(cfg.jump_p);
     sc.sigma = cfg.sigma;
     sc.nsig1 = -cfg.sigma;
-    sc.nsig2 = -2.0f * cfg.sigma;
+    sc.sigma23 = cfg.sigma * 0x1p-23f;
     prep_elites_kernel<<<unit_blocks(static_cast<uint64_t>(ne + 1) * kNtot, 256), 256, 0, st>>>(
         d_genomes, ne, tab, ids, tribes);
     CSX_CUDA(cudaGetLastError());

@@ -140,7 +140,7 @@ def test_branch_probabilities(orc, env, imm, jump):
     check(orc, 30_000, 40, 21, 4, wl.surrogate_161(), wl.seeded_elites(64), imm=imm, jump=jump)
 
 
-@pytest.mark.parametrize("sigma", [0.0, 0.5, 1e-30, 2.0, 3e38, float("inf"), float("nan"), -0.25])
+@pytest.mark.parametrize("sigma", [0.0, 0.5, 1e-30, 1e-31, 2e-40, 2.0, 3e38, float("inf"), float("nan"), -0.25])
 def test_sigma(orc, sigma):
     from codec_arena_gb300 import workloads as wl
 
