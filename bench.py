@@ -212,7 +212,9 @@ def main():
 
     el = wl.seeded_elites(N_ELITES)
     model = screen.Model.from_compact(wl.surrogate_161())
-    seed = SEED if world == 1 else SEED * 1000003 + rank * 131  # one island per rank
+    from codec_arena_gb300 import parallel
+
+    seed = SEED if world == 1 else parallel.island_seed(SEED, rank)  # one island per rank
     cfg = screen.Cfg(args.lam, args.keep, seed, threads=args.threads, flags=_lib.FLAG_STAGE_TIMES)
     d_el = torch.from_numpy(el.view(np.uint8).copy()).cuda()
     d_out = torch.zeros(args.keep * _lib.SURVIVOR_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
@@ -255,10 +257,7 @@ def main():
     clocks = sampler.stop()
     step_ms = [a.elapsed_time(b) for a, b in ev]
     t_dev = sum(step_ms) / 1000.0
-    if world > 1:
-        t = torch.tensor([t_dev], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_dev = float(t.item())
+    t_dev = parallel.max_over_ranks(t_dev, device="cuda")
     value = world * args.lam * args.steps / t_dev
     launches = stage[-1]["launches"]
 
@@ -270,10 +269,7 @@ def main():
     for _ in range(e2e_steps):
         surv, scr = screen.screen(hcfg, model, el)
     e2e_t = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_t], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_t = float(t.item())
+    e2e_t = parallel.max_over_ranks(e2e_t, device="cuda")
     e2e = {"value": world * args.lam * e2e_steps / e2e_t, "unit": "candidates/s",
            "h2d_bytes_per_step": int(el.nbytes + ctypes.sizeof(_lib.CsxModel) + ctypes.sizeof(_lib.CsxCfg)),
            "d2h_bytes_per_step": int(len(surv) * _lib.SURVIVOR_DTYPE.itemsize + 32),

@@ -1,0 +1,48 @@
+"""Worker for tests/test_parallel.py, launched by torch.distributed.run with
+the gloo backend on CPU. Each rank screens its share of one generation's RNG
+streams with the CPU oracle (the checker stands in for the GPU engine here),
+then the ranks merge survivors and agree on the slowest rank's time."""
+import json
+import os
+import sys
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(os.path.dirname(HERE), "oracle"))
+
+import numpy as np  # noqa: E402
+import torch.distributed as dist  # noqa: E402
+
+import oracle  # noqa: E402
+from codec_arena_gb300 import parallel, workloads as wl  # noqa: E402
+
+
+def main():
+    dist.init_process_group("gloo")
+    rank, world = dist.get_rank(), dist.get_world_size()
+    lam, keep, seed, T = int(sys.argv[1]), int(sys.argv[2]), int(sys.argv[3]), int(sys.argv[4])
+    out = sys.argv[5]
+    el = wl.seeded_elites(16, seed=3)
+    m = oracle.model_from_compact(wl.surrogate_161())
+    c = oracle.cfg(lam, keep, seed, threads=T)
+    Tn = max(1, min(T, lam))
+    per = lam // Tn
+    t0 = time.perf_counter()
+    local = []
+    for t in parallel.stream_ranges(T, lam, world)[rank]:
+        my = lam - (Tn - 1) * per if t == Tn - 1 else per
+        d = oracle.stream_dump(c, m, el, t, my)
+        d["index"] = np.arange(my)
+        local.append(d)
+    mine = parallel.merge_survivors(local, keep)
+    merged = parallel.gather_survivors(mine, keep)
+    slowest = parallel.max_over_ranks(time.perf_counter() - t0 + rank)
+    if rank == 0:
+        with open(out, "w") as f:
+            json.dump({"merged": merged.tobytes().hex(), "slowest": slowest, "world": world}, f)
+    dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

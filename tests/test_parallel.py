@@ -1,0 +1,68 @@
+"""Multi-rank host logic on CPU (gloo, world size 2): stream sharding of one
+generation and island seeding, checked against the single-process oracle."""
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def test_island_seed_matches_evolve():
+    from codec_arena_gb300 import parallel
+
+    # brain/evolve.py:437: --seed args.seed * 1000003 + args.shard * 131 + gen
+    assert parallel.island_seed(42, 7, 3) == 42 * 1000003 + 7 * 131 + 3
+
+
+def test_stream_ranges_cover_all_streams():
+    from codec_arena_gb300 import parallel
+
+    for T, lam, w in [(4, 10**9, 2), (4, 10**9, 3), (7, 100, 8), (100, 5, 2), (0, 10, 2)]:
+        rs = parallel.stream_ranges(T, lam, w)
+        flat = [t for r in rs for t in r]
+        assert flat == list(range(max(1, min(T, lam))))
+
+
+def test_merge_equals_single_process(orc):
+    from codec_arena_gb300 import parallel, workloads as wl
+
+    el = wl.seeded_elites(16, seed=3)
+    m = orc.model_from_compact(wl.surrogate_161())
+    lam, keep, T = 20_005, 50, 6
+    c = orc.cfg(lam, keep, 9, threads=T)
+    full, _ = orc.screen(c, m, el)
+    parts = []
+    for rg in parallel.stream_ranges(T, lam, 3):
+        local = []
+        for t in rg:
+            my = lam - (T - 1) * (lam // T) if t == T - 1 else lam // T  # last stream: the remainder
+            d = orc.stream_dump(c, m, el, t, my)
+            d["index"] = np.arange(my)
+            local.append(d)
+        parts.append(parallel.merge_survivors(local, keep))
+    assert parallel.merge_survivors(parts, keep).tobytes() == full.tobytes()
+
+
+def test_gloo_world_size_2(orc, tmp_path):
+    from codec_arena_gb300 import _lib
+
+    out = tmp_path / "rank0.json"
+    lam, keep, seed, T = 12_000, 40, 5, 4
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=2",
+           "--master-addr=127.0.0.1", "--master-port=29533",
+           os.path.join(ROOT, "tests", "_dist_worker.py"), str(lam), str(keep), str(seed), str(T), str(out)]
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=300, env=env)
+    assert r.returncode == 0, r.stderr[-2000:]
+    res = json.load(open(out))
+    assert res["world"] == 2 and res["slowest"] >= 1.0  # rank 1 adds 1 s: the max is taken
+    merged = np.frombuffer(bytes.fromhex(res["merged"]), dtype=_lib.SURVIVOR_DTYPE)
+    from codec_arena_gb300 import workloads as wl
+
+    full, _ = orc.screen(orc.cfg(lam, keep, seed, threads=T), orc.model_from_compact(wl.surrogate_161()),
+                         wl.seeded_elites(16, seed=3))
+    assert merged.tobytes() == full.tobytes()
