@@ -1,0 +1,153 @@
+"""The screen step of brain/evolve.py, in process, and its file formats.
+
+`screen_generation` replaces the subprocess call at brain/evolve.py:419-454:
+it takes the elite dicts evolve.py keeps in memory, runs the GPU screen and
+returns promoted dicts (pa, pb, tribe, g) plus the screened count, without
+writing elites.txt or reading promoted.txt. With `text_roundtrip=True` the
+elites go through the same text the subprocess path uses (genome_line, then
+the screen's own parser, including its v6 quirk unless `v6_fix`), and the
+promoted genes come back rounded to 4 decimals as evolve.py reads them; the
+result then equals the file-based path exactly.
+
+The format helpers mirror evolve.py's own: `load_pop` (:71-101),
+`genome_line` (:104-106), `features` (:211-220), `load_weights` (:223-241),
+`save_weights` (:244-247).
+"""
+from __future__ import annotations
+
+from typing import Dict, List, Sequence, Tuple
+
+import numpy as np
+
+from . import genome as _genome
+from . import parallel as _parallel
+from . import screen as _screen
+from ._lib import GENOME_DTYPE
+
+NG_EFF, NR_REG = 23, 6
+NG = NG_EFF + NR_REG
+REG_DEFAULT = 0.5
+NEW_GENE_DEFAULT = 0.0
+N_NEW = 7
+
+
+def load_pop(path: str) -> List[Dict]:
+    """brain/evolve.py:71-101: pop lines of 21/27/29/32/33/34 tokens migrated
+    to 34 tokens (5 + 29 genes); other widths are skipped."""
+    pop = []
+    with open(path) as f:
+        for line in f:
+            line = line.strip()
+            if not line or line.startswith("#"):
+                continue
+            t = line.split()
+            if len(t) == 5 + 16:
+                t = t + [str(NEW_GENE_DEFAULT)] * N_NEW + [str(REG_DEFAULT)] * NR_REG
+            elif len(t) == 5 + 22:
+                t = t[: 5 + 16] + [str(NEW_GENE_DEFAULT)] * N_NEW + t[5 + 16:]
+            elif len(t) == 5 + 24:
+                t = t[: 5 + 18] + [str(NEW_GENE_DEFAULT)] * 5 + t[5 + 18:]
+            elif len(t) == 5 + 27:
+                t = t[: 5 + 21] + [str(NEW_GENE_DEFAULT)] * 2 + t[5 + 21:]
+            elif len(t) == 5 + 28:
+                t = t[: 5 + 22] + [str(NEW_GENE_DEFAULT)] + t[5 + 22:]
+            if len(t) != 5 + NG:
+                continue
+            pop.append({"id": int(t[0]), "gen": int(t[1]), "pa": int(t[2]), "pb": int(t[3]),
+                        "tribe": int(t[4]), "g": [float(x) for x in t[5:]]})
+    return pop
+
+
+def genome_line(g: Dict) -> str:
+    """brain/evolve.py:104-106."""
+    return f"{g['id']} {g['gen']} {g['pa']} {g['pb']} {g['tribe']} " + " ".join(f"{x:.4f}" for x in g["g"])
+
+
+def features(genes) -> np.ndarray:
+    """brain/evolve.py:211-220, vectorised: (n, 29) genes -> (n, 166) features
+    [1 | 29 linear | g_i g_j for j <= i < 16]."""
+    g = np.atleast_2d(np.asarray(genes, dtype=np.float64))
+    ii, jj = np.tril_indices(16)  # row-major: i outer, j <= i inner
+    quad = g[:, ii] * g[:, jj]
+    return np.concatenate([np.ones((g.shape[0], 1)), g, quad], axis=1)
+
+
+def load_weights(path: str) -> List[float]:
+    """brain/evolve.py:223-241: any compact layout migrated to 166."""
+    with open(path) as f:
+        toks = f.read().split()
+    n = int(toks[0])
+    w = [float(x) for x in toks[1:1 + n]]
+    if n == 153:
+        w = w[:17] + [0.0] * 13 + w[17:]
+    elif n == 159:
+        w = w[:17] + [0.0] * 7 + w[17:]
+    elif n == 161:
+        w = w[:19] + [0.0] * 5 + w[19:]
+    elif n == 164:
+        w = w[:22] + [0.0] * 2 + w[22:]
+    elif n == 165:
+        w = w[:29] + [0.0] + w[29:]
+    return w
+
+
+def save_weights(path: str, w: Sequence[float]) -> None:
+    """brain/evolve.py:244-247."""
+    with open(path, "w") as f:
+        f.write(f"{len(w)}\n")
+        f.write(" ".join(f"{x:.8e}" for x in w) + "\n")
+
+
+def elites_array(elites: Sequence[Dict], text_roundtrip: bool = False, v6_fix: bool = False) -> np.ndarray:
+    """Elite dicts -> GENOME_DTYPE records, directly or through elites.txt text."""
+    if text_roundtrip:
+        return _genome.load_elites_text("".join(genome_line(g) + "\n" for g in elites), v6_fix=v6_fix)
+    out = np.zeros(len(elites), dtype=GENOME_DTYPE)
+    for i, g in enumerate(elites):
+        out[i]["id"], out[i]["gen"], out[i]["pa"], out[i]["pb"], out[i]["tribe"] = (
+            g["id"], g["gen"], g["pa"], g["pb"], g["tribe"])
+        out[i]["g"] = np.asarray(g["g"], dtype=np.float32)
+    return out
+
+
+def screen_generation(elites: Sequence[Dict], model, *, screens: int, keep: int, seed: int, shard: int,
+                      gen: int, threads: int = 4, sigma_decay: float = 0.93, jump: float = 0.02,
+                      imm: float = 0.01, text_roundtrip: bool = False,
+                      v6_fix: bool = False) -> Tuple[List[Dict], int]:
+    """One generation's screen as brain/evolve.py:431-454 runs it, in process.
+
+    `model` is a screen.Model or compact weights. Returns (promoted, screened):
+    promoted dicts carry pa, pb, tribe and the 29 genes, best first.
+    """
+    if not isinstance(model, _screen.Model):
+        model = _screen.Model.from_compact(np.asarray(model, dtype=np.float32))
+    sigma = 0.12 * (sigma_decay ** gen)
+    if text_roundtrip:  # evolve.py passes sigma as "%.4f" text
+        sigma = float(f"{sigma:.4f}")
+    cfg = _screen.Cfg(int(screens), int(keep), _parallel.island_seed(seed, shard, gen), threads=int(threads),
+                      sigma=sigma, jump_p=jump, imm_p=imm)
+    surv, screened = _screen.screen(cfg, model, elites_array(elites, text_roundtrip, v6_fix))
+    promoted = []
+    for r in surv:
+        g = [float(x) for x in r["g"]]
+        if text_roundtrip:
+            g = [float(f"{x:.4f}") for x in g]
+        promoted.append({"id": 0, "gen": 0, "pa": int(r["pa"]), "pb": int(r["pb"]), "tribe": int(r["tribe"]),
+                         "g": g})
+    return promoted, screened
+
+
+def next_population(elites: Sequence[Dict], promoted: Sequence[Dict], *, shard: int, gen: int, pop: int,
+                    keep: int) -> List[Dict]:
+    """brain/evolve.py:455-461: elites first, then up to `keep` promoted genomes
+    with the ids and generation evolve.py assigns. The caller tops the list up
+    to `pop` with its own tournament breeding (:462-474)."""
+    nxt = [dict(g) for g in elites]
+    for p in list(promoted)[:keep]:
+        nxt.append({"id": shard * 10_000_000 + gen * pop + len(nxt), "gen": gen + 1, "pa": p["pa"],
+                    "pb": p["pb"], "tribe": p["tribe"], "g": list(p["g"])})
+    return nxt
+
+
+__all__ = ["load_pop", "genome_line", "features", "load_weights", "save_weights", "elites_array",
+           "screen_generation", "next_population"]
