@@ -112,6 +112,22 @@ SIGNATURES = {
     "csx_last_run_info": (ctypes.c_int, [ctypes.POINTER(CsxRunInfo)]),
 }
 
+# include/csx_surrogate.h (same library); device pointers and the stream as void*.
+_vp, _i64, _int = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int
+SURROGATE_SIGNATURES = {
+    "csx_sg_workspace_bytes": (_u64, [_int]),
+    "csx_sg_forward": (_int, [_vp, _int, _vp, _i64, _int, _int, _vp, _vp]),
+    "csx_sg_forward_f64": (_int, [_vp, _int, _vp, _i64, _int, _vp, _vp]),
+    "csx_sg_backward": (_int, [_vp, _int, _vp, _i64, _int, _int, _vp, _vp, _vp, _vp, _vp]),
+    "csx_sg_backward_coef_f64": (_int, [_int, _vp, _i64, _int, _vp, _vp, _vp, _vp]),
+    "csx_sg_normal_equations": (_int, [_int, _vp, _i64, _int, _vp, _vp, _vp, _vp, _vp]),
+    "csx_sg_ridge_solve": (_int, [_int, _vp, _vp, ctypes.c_double, _vp, _vp, _vp, _vp]),
+    "csx_sg_ascend": (_int, [_vp, _int, _vp, _i64, _int, _f32, _int, _vp, _vp]),
+}
+SIGNATURES.update(SURROGATE_SIGNATURES)
+
+SG_FP32, SG_BF16, SG_FP64 = 0, 1, 2
+
 _lib = None
 
 

@@ -31,10 +31,11 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
               "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include")]
 
-UNITS = [  # (source, compiler)
-    ("csx_screen.cu", "nvcc"),
-    ("csx_host.cpp", "g++"),
-    ("csx_bench.cu", "nvcc"),
+UNITS = [  # (source, compiler, library)
+    ("csx_screen.cu", "nvcc", LIB),
+    ("csx_host.cpp", "g++", LIB),
+    ("csx_surrogate.cu", "nvcc", LIB),
+    ("csx_bench.cu", "nvcc", BENCH_LIB),
 ]
 
 
@@ -47,8 +48,8 @@ def _compile(src: str, kind: str, verbose: bool) -> str:
     os.makedirs(BUILD, exist_ok=True)
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
     path = os.path.join(CSRC, src)
-    deps = [path, os.path.join(CSRC, "csx_device.cuh"), os.path.join(ROOT, "include", "csx_screen.h"),
-            os.path.join(ROOT, "include", "csx_bench.h")]
+    deps = [path, os.path.join(CSRC, "csx_device.cuh")] + [
+        os.path.join(ROOT, "include", h) for h in ("csx_screen.h", "csx_surrogate.h", "csx_bench.h")]
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
         return obj
     if kind == "nvcc":
@@ -68,7 +69,8 @@ def build(verbose: bool = False) -> str:
     """Compile every translation unit (in parallel) and link the library and CLI."""
     with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         objs = list(ex.map(lambda u: _compile(u[0], u[1], verbose), UNITS))
-    for lib_path, lib_objs in ((LIB, objs[:2]), (BENCH_LIB, objs[2:])):
+    for lib_path in (LIB, BENCH_LIB):
+        lib_objs = [o for o, u in zip(objs, UNITS) if u[2] == lib_path]
         newest = max(os.path.getmtime(o) for o in lib_objs)
         if not os.path.exists(lib_path) or os.path.getmtime(lib_path) < newest:
             tmp = lib_path + f".tmp{os.getpid()}"

@@ -71,3 +71,18 @@ def load_compact(path: str) -> np.ndarray:
 def surrogate_161() -> np.ndarray:
     """The reference's committed v3 surrogate (161 coefficients), from the fixture."""
     return load_compact(SURROGATE_161)
+
+
+def refit_table(n: int = 400_000, seed: int = 5, ng: int = 16, noise: float = 0.5):
+    """Synthetic refit table: n rows of `ng` genes uniform in [0, 1] (f32),
+    targets = a seeded ground-truth quadratic (N(0, 1) coefficients, FP64) plus
+    Student-t(3) noise of scale `noise`. Returns (genes, fit, w_true)."""
+    rng = np.random.default_rng(seed)
+    genes = rng.random((n, ng), dtype=np.float32)
+    nf = 1 + ng + 136
+    w_true = rng.normal(0.0, 1.0, nf)
+    g = genes.astype(np.float64)
+    ii, jj = np.tril_indices(16)
+    fit = w_true[0] + g @ w_true[1:1 + ng] + (g[:, ii] * g[:, jj]) @ w_true[1 + ng:]
+    fit = fit + noise * rng.standard_t(3, n)
+    return genes, fit, w_true

@@ -10,13 +10,15 @@ import pytest
 
 from conftest import ROOT, has_gpu
 
-HEADER = os.path.join(ROOT, "include", "csx_screen.h")
+HEADERS = [os.path.join(ROOT, "include", h) for h in ("csx_screen.h", "csx_surrogate.h")]
 
 
 def declared_functions():
-    src = open(HEADER).read()
-    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"\b(csx_[a-z0-9_]+)\s*\(", src)))
+    names = set()
+    for h in HEADERS:
+        src = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        names |= set(re.findall(r"\b(csx_[a-z0-9_]+)\s*\(", src))
+    return sorted(names)
 
 
 def test_header_declares_expected_api():

@@ -4,12 +4,18 @@ Pins, each citing the reference test it restates:
   * splitmix64: the published output sequence of seed 0;
   * Model.fromCompact layout: src/screen.zig:345-377;
   * Model.score monotonicity and neutrality: src/screen.zig:379-405;
-  * parseLine / formatLine: src/genome.zig:296-372.
+  * parseLine / formatLine: src/genome.zig:296-372;
+  * the surrogate refit (oracle/refit.py): outputs of brain/evolve.py's own
+    features / refit_surrogate (tests/golden/evolve_golden.json).
 Where a reference assertion contradicts the reference code, the test asserts
 what the code computes and names the assertion it departs from.
 """
+import os
+
 import numpy as np
 import pytest
+
+from conftest import ROOT
 
 
 def test_splitmix64_published_sequence(orc):
@@ -243,3 +249,22 @@ def test_oracle_heap_tie_semantics(orc):
     got, _ = orc.screen(orc.cfg(4000, 20, 5, threads=4), m, el)
     assert list(got["stream"]) == [0] * 20
     assert list(got["index"]) == list(range(20))
+
+
+def test_refit_oracle_pinned_to_reference_refit():
+    """oracle/refit.py against brain/evolve.py's own refit_surrogate output
+    (400 seeded rows, alpha 50, written with "%.8e")."""
+    import json
+
+    import refit
+
+    with open(os.path.join(ROOT, "tests", "golden", "evolve_golden.json")) as f:
+        d = json.load(f)
+    r = d["refit"]
+    assert r["written"]
+    for solve in (refit.refit_solve, refit.refit_cholesky):
+        w = solve(r["rows_genes"], r["rows_fit"], r["prior"], r["alpha"])
+        np.testing.assert_allclose(w, r["weights"], rtol=1e-8, atol=1e-9)
+    np.testing.assert_array_equal(refit.features(d["genes"]), np.asarray(d["features"]))
+    # fewer than 300 rows: the reference writes nothing (brain/evolve.py:257)
+    assert len(r["rows_genes"]) >= 300
