@@ -57,6 +57,9 @@ def parse():
     ap.add_argument("--keep", type=int, default=KEEP)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="generation", choices=["generation", "islands"],
+                    help="islands: 20 islands batched in one graph launch (not the headline line)")
+    ap.add_argument("--islands", type=int, default=20)
     return ap.parse_args()
 
 
@@ -191,10 +194,83 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_islands(args):
+    """Batched islands: `args.islands` islands (budgets log-uniform in [1e8,
+    2.65e9], 16..256 elites, own seeded N(0, 0.1) 153-term surfaces, top-K in
+    {32, 128, 256}, T = 4) screened by one graph launch of the batch pipeline
+    per step, tunables from the autotuner. Reported beside the same islands
+    run as separate single-island screens."""
+    import numpy as np
+    import torch
+
+    from codec_arena_gb300 import autotune, islands, screen, workloads as wl
+
+    torch.cuda.set_device(0)
+    isl = wl.seeded_islands(args.islands)
+    cfgs = [screen.Cfg(d["lambda"], d["keep"], d["seed"], threads=d["threads"]) for d in isl]
+    models = [screen.Model.from_compact(d["weights"]) for d in isl]
+    elites = [d["elites"] for d in isl]
+    total = sum(c.lambda_ for c in cfgs)
+    t0 = time.perf_counter()
+    best, table = autotune.autotune(cfgs, models, elites, scale=0.1, reps=2)
+    tune_s = time.perf_counter() - t0
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(max(3, args.warmup)):
+        islands.screen_batch(cfgs, models, elites, tune=best)
+    sampler = ClockSampler(0)
+    sampler.start()
+    dev_ms, wall = [], []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        res = islands.screen_batch(cfgs, models, elites, tune=best)
+        wall.append(time.perf_counter() - t)
+        dev_ms.append(islands.last_batch_info()["ms_device"])
+    clocks = sampler.stop()
+    info = islands.last_batch_info()
+    assert all(n == c.lambda_ for (_, n), c in zip(res, cfgs))
+    # the same islands as separate screens (device API, CUDA events)
+    d_res = torch.zeros(4, dtype=torch.int64, device="cuda")
+    seq_ms = 0.0
+    for c, m, e in zip(cfgs, models, elites):
+        d_el = torch.from_numpy(e.view(np.uint8).copy()).cuda()
+        d_out = torch.zeros(c.keep * 168, dtype=torch.uint8, device="cuda")
+        screen.screen_device(c, m, d_el, d_out, d_res)
+        flush.fill_(1)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        screen.screen_device(c, m, d_el, d_out, d_res)
+        b.record()
+        b.synchronize()
+        seq_ms += a.elapsed_time(b)
+    ms = statistics.mean(dev_ms)
+    line = {"metric": "candidates/sec (batched islands, 1 GB300)", "value": total / (ms / 1000.0),
+            "unit": "candidates/s", "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup),
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u64/f32", "data": "synthetic (seeded)",
+            "config": {"workload": f"{len(cfgs)} islands in one graph launch: budgets log-uniform 1e8..2.65e9 "
+                                   f"(total {total}), 16..256 seeded elites, seeded N(0,0.1) 153-term surfaces, "
+                                   "top-K in {32,128,256}, T=4",
+                       "islands": [[c.lambda_, c.keep, int(e.shape[0])] for c, e in zip(cfgs, elites)],
+                       "l2": "flushed between steps (256 MiB write)"},
+            "e2e": {"value": total / statistics.mean(wall), "unit": "candidates/s",
+                    "h2d_bytes_per_step": int(sum(e.nbytes for e in elites)),
+                    "d2h_bytes_per_step": int(sum(len(r[0]) for r in res) * 168),
+                    "api": "csx_screen_batch (host buffers; capture/update + graph launch + copies)"},
+            "sequential_single_screens": {"ms": seq_ms, "value": total / (seq_ms / 1000.0)},
+            "tune": {"chosen": [best.item_cands, best.seg_cands, best.ctas_per_sm], "tuning_s": tune_s,
+                     "table_ms": [[[t.item_cands, t.seg_cands, t.ctas_per_sm], ms_] for t, ms_ in table]},
+            "graph": info, "clocks": clocks, "gpu_launches": int(info["launches"]) * args.steps}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "islands":
+        return run_islands(args)
     import numpy as np
     import torch
 
@@ -313,7 +389,8 @@ def main():
             "config": workload_config(args, world), "e2e": e2e, "roofline": roofline,
             "clocks": clocks, "gpu_launches": int(launches * args.steps),
             "stages_ms_last_step": {k: round(v, 4) for k, v in stage[-1].items() if k.startswith("ms_")},
-            "shape": {k: stage[-1][k] for k in ("screen_ctas", "segments", "seg_draws", "item_cands")},
+            "shape": dict({k: stage[-1][k] for k in ("screen_ctas", "segments", "seg_draws", "item_cands")},
+                          items=int(res[3])),
             "exact_evals_last_step": stage[-1]["exact_evals"],
             "wall_s": wall}
     if world == 1 and not args.no_cpu_baseline:

@@ -126,6 +126,27 @@ SURROGATE_SIGNATURES = {
 }
 SIGNATURES.update(SURROGATE_SIGNATURES)
 
+MAX_ISLANDS = 64
+
+
+class CsxBatchTune(ctypes.Structure):
+    _fields_ = [("item_cands", _u32), ("seg_cands", _u32), ("ctas_per_sm", _u32), ("reserved", _u32)]
+
+
+class CsxBatchInfo(ctypes.Structure):
+    _fields_ = [("islands", _u32), ("launches", _u32), ("screen_ctas", _u32), ("graph_nodes", _u32),
+                ("ms_capture", _f32), ("ms_device", _f32)]
+
+
+SIGNATURES.update({
+    "csx_screen_batch": (_int, [_int, ctypes.POINTER(CsxCfg), ctypes.POINTER(CsxModel), _vp,
+                                ctypes.POINTER(_int), ctypes.POINTER(CsxBatchTune), _vp, ctypes.POINTER(_u64),
+                                ctypes.POINTER(_u64)]),
+    "csx_screen_batch_device": (_int, [_int, ctypes.POINTER(CsxCfg), ctypes.POINTER(CsxModel), _vp,
+                                       ctypes.POINTER(_int), ctypes.POINTER(CsxBatchTune), _vp, _vp, _vp]),
+    "csx_last_batch_info": (_int, [ctypes.POINTER(CsxBatchInfo)]),
+})
+
 SG_FP32, SG_BF16, SG_FP64 = 0, 1, 2
 
 _lib = None

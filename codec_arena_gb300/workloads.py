@@ -86,3 +86,22 @@ def refit_table(n: int = 400_000, seed: int = 5, ng: int = 16, noise: float = 0.
     fit = w_true[0] + g @ w_true[1:1 + ng] + (g[:, ii] * g[:, jj]) @ w_true[1 + ng:]
     fit = fit + noise * rng.standard_t(3, n)
     return genes, fit, w_true
+
+
+def seeded_islands(n: int = 20, seed: int = 4, lam_lo: float = 1e8, lam_hi: float = 2.65e9,
+                   ne_lo: int = 16, ne_hi: int = 256, keeps=(32, 128, 256), threads: int = 4):
+    """Batched-islands workload: n islands with log-uniform budgets in
+    [lam_lo, lam_hi], elite pools of ne_lo..ne_hi seeded genomes, each island
+    with its own seeded N(0, 0.1) 153-coefficient surface and a top-K from
+    `keeps`. Returns a list of dicts (lambda, keep, seed, threads, elites,
+    weights)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        lam = int(round(float(np.exp(rng.uniform(np.log(lam_lo), np.log(lam_hi))))))
+        ne = int(rng.integers(ne_lo, ne_hi + 1))
+        keep = int(keeps[int(rng.integers(0, len(keeps)))])
+        out.append({"lambda": lam, "keep": keep, "seed": 100 + i, "threads": threads,
+                    "elites": seeded_elites(ne, seed=1000 + i),
+                    "weights": seeded_normal_model(seed=2000 + i)})
+    return out

@@ -139,7 +139,7 @@ int csx_screen(const csx_cfg *cfg, const csx_model *model, const csx_genome *eli
 /* Same, with device-resident elites and survivors, enqueued on `cuda_stream`
  * (a cudaStream_t; NULL = the legacy default stream). d_result receives four
  * device uint64: survivor count, screened count, device error bits (0 = ok)
- * and a reserved word. The call returns after enqueueing; calls on different
+ * and the number of work items screened. The call returns after enqueueing; calls on different
  * streams are ordered after one another by the library. */
 int csx_screen_device(const csx_cfg *cfg, const csx_model *model, const csx_genome *d_elites,
                       int n_elites, csx_survivor *d_out, uint64_t out_cap, uint64_t *d_result,
@@ -189,6 +189,53 @@ typedef struct csx_run_info {
     uint64_t exact_evals;   /* candidates scored in the reference order (filter mode) */
 } csx_run_info;
 int csx_last_run_info(csx_run_info *out);
+
+/* ---- batched islands --------------------------------------------------------
+ * Several independent screens ("islands": the reference's CI shards, each
+ * running brain/evolve.py with its own seed, elites and surrogate,
+ * .github/workflows/arena.yml:56-92) in one pipeline: every island's work
+ * items are built on its own forked stream, then ONE persistent screen launch
+ * consumes all islands' items and keeps a top-K per island, then one merge
+ * tree and one regeneration launch serve all islands. Results per island
+ * equal csx_screen's for that island's cfg, model and elites.
+ *
+ * Tunables do not change results, only speed (0 = automatic). */
+#define CSX_MAX_ISLANDS 64
+typedef struct csx_batch_tune {
+    uint32_t item_cands;  /* candidates per work item, rounded down to a power of two */
+    uint32_t seg_cands;   /* candidates per walk segment */
+    uint32_t ctas_per_sm; /* persistent screen CTAs per SM (1..3) */
+    uint32_t reserved;
+} csx_batch_tune;
+
+/* Per-island timing of the last batch call on this device. */
+typedef struct csx_batch_info {
+    uint32_t islands;
+    uint32_t launches;    /* kernels in the batch pipeline */
+    uint32_t screen_ctas;
+    uint32_t graph_nodes; /* nodes of the captured graph (host call) */
+    float ms_capture;     /* host: stream capture + instantiate/update */
+    float ms_device;      /* device time of the graph launch (host call) */
+} csx_batch_info;
+
+/* Host buffers. elites: all islands' genomes back to back (island i has
+ * n_elites[i]); out: island i's survivors at offset sum_{j<i} keep_j;
+ * n_out / screened: one per island. The pipeline is captured into a CUDA
+ * graph and launched once. */
+int csx_screen_batch(int n_islands, const csx_cfg *cfgs, const csx_model *models, const csx_genome *elites,
+                     const int *n_elites, const csx_batch_tune *tune, csx_survivor *out, uint64_t *n_out,
+                     uint64_t *screened);
+
+/* Device buffers (same layout; d_result holds 4 words per island: count,
+ * screened, error bits, items), enqueued on `cuda_stream` without a graph.
+ * Not for stream capture (returns CSX_ERR_BAD_ARGS on a capturing stream):
+ * its island descriptors come from a host staging area that the next batch
+ * call reuses; csx_screen_batch captures and launches its own graph. */
+int csx_screen_batch_device(int n_islands, const csx_cfg *cfgs, const csx_model *models,
+                            const csx_genome *d_elites, const int *n_elites, const csx_batch_tune *tune,
+                            csx_survivor *d_out, uint64_t *d_result, void *cuda_stream);
+
+int csx_last_batch_info(csx_batch_info *out);
 
 #ifdef __cplusplus
 }

@@ -217,7 +217,8 @@ def test_refit_matches_reference_golden():
     genes = torch.tensor(r["rows_genes"], dtype=torch.float64)
     # the reference computes features from f64 genes; these rows are f32-exact only after rounding
     g32 = genes.float()
-    w = surrogate.refit(g32.cuda(), torch.tensor(r["rows_fit"]).cuda(), torch.tensor(r["prior"]).cuda(), r["alpha"])
+    f64 = dict(dtype=torch.float64, device="cuda")
+    w = surrogate.refit(g32.cuda(), torch.tensor(r["rows_fit"], **f64), torch.tensor(r["prior"], **f64), r["alpha"])
     import refit
 
     want = refit.refit_cholesky(g32.numpy(), r["rows_fit"], r["prior"], r["alpha"])
