@@ -145,7 +145,9 @@ SIGNATURES.update({
     "csx_screen_batch_device": (_int, [_int, ctypes.POINTER(CsxCfg), ctypes.POINTER(CsxModel), _vp,
                                        ctypes.POINTER(_int), ctypes.POINTER(CsxBatchTune), _vp, _vp, _vp]),
     "csx_last_batch_info": (_int, [ctypes.POINTER(CsxBatchInfo)]),
+    "csx_tc_score": (_int, [ctypes.POINTER(CsxModel), _int, _vp, _i64, _int, _vp, _vp, _vp]),
 })
+TC_BF16, TC_FP16 = 1, 2
 
 SG_FP32, SG_BF16, SG_FP64 = 0, 1, 2
 

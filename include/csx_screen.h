@@ -237,6 +237,21 @@ int csx_screen_batch_device(int n_islands, const csx_cfg *cfgs, const csx_model 
 
 int csx_last_batch_info(csx_batch_info *out);
 
+/* ---- precision form (tensor cores) -------------------------------------------
+ * No counterpart in the reference, which scores in FP32 only. The quadratic
+ * block over the 16 legacy genes runs on the tensor cores (tcgen05.mma, FP32
+ * accumulation in tensor memory) with the genes in BF16 (x = g) or FP16 with
+ * the per-gene map x' = 2g - 1 onto [-1, 1]; constant and linear terms stay
+ * FP32 on the exact genes. */
+#define CSX_TC_BF16 1
+#define CSX_TC_FP16 2
+
+/* Score n genomes (rows of ldg >= 29 floats, device) in the precision form.
+ * *d_err (device, zeroed by the caller) receives error bits (16: a
+ * tensor-core completion wait gave up). Asynchronous on `cuda_stream`. */
+int csx_tc_score(const csx_model *model, int form, const float *d_genes, int64_t n, int ldg, float *d_out,
+                 uint32_t *d_err, void *cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

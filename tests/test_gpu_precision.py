@@ -1,0 +1,81 @@
+"""Precision form: tensor-core (tcgen05) scoring in BF16 / FP16 against a
+numpy emulation of the same rounded inputs (tight: only FP32 accumulation
+differs) and against the FP64 score (the error the form trades)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu(csx):
+    from conftest import has_gpu
+
+    if not has_gpu():
+        pytest.skip("no CUDA device")
+
+
+def _round(x, form):
+    import torch
+
+    t = torch.from_numpy(np.asarray(x, dtype=np.float32))
+    return t.to(torch.bfloat16 if form == "bf16" else torch.float16).to(torch.float64).numpy()
+
+
+def _emulate(model, g, form):
+    """FP64 evaluation of the precision form on the same rounded operands."""
+    g = g.astype(np.float64)
+    w0, lin, q = float(model.w0), model.w_lin.astype(np.float64), model.w_quad.astype(np.float64).reshape(16, 16)
+    L = np.tril(q)
+    s = 16 * w0 + g @ lin
+    if form == "bf16":
+        x = _round(g[:, :16], "bf16")
+        y = x @ _round(L, "bf16").T
+        return s + np.sum(g[:, :16] * y, axis=1), np.abs(16 * w0) + np.abs(g) @ np.abs(lin) + \
+            np.sum(np.abs(g[:, :16]) * (np.abs(x) @ np.abs(L).T), axis=1)
+    xp = 2 * g[:, :16] - 1
+    u = (L.sum(axis=1) + L.sum(axis=0)) / 4
+    v = L.sum() / 4
+    c = 16 * w0 + v - u.sum()
+    lin2 = lin.copy()
+    lin2[:16] += 2 * u
+    cf = np.float32(c).astype(np.float64)
+    lf = lin2.astype(np.float32).astype(np.float64)
+    y = _round(xp, "fp16") @ _round(L / 4, "fp16").T
+    A = np.abs(cf) + np.abs(g) @ np.abs(lf) + np.sum(np.abs(xp) * (np.abs(xp) @ np.abs(L / 4).T), axis=1)
+    return cf + g @ lf + np.sum(xp * y, axis=1), A
+
+
+def _fp64(model, g):
+    g = g.astype(np.float64)
+    L = np.tril(model.w_quad.astype(np.float64).reshape(16, 16))
+    return 16 * float(model.w0) + g @ model.w_lin.astype(np.float64) + np.einsum("ni,ij,nj->n", g[:, :16], L, g[:, :16])
+
+
+@pytest.mark.parametrize("form", ["bf16", "fp16"])
+@pytest.mark.parametrize("which", ["v3", "normal"])
+def test_tc_score_matches_emulation_and_bounds(form, which):
+    import torch
+
+    from codec_arena_gb300 import precision, screen, workloads as wl
+
+    w = wl.surrogate_161() if which == "v3" else wl.seeded_normal_model(seed=2)
+    m = screen.Model.from_compact(w)
+    rng = np.random.default_rng(3)
+    n = 100_003
+    g = rng.random((n, 29), dtype=np.float32)
+    got = precision.tc_score(m, torch.from_numpy(g).cuda(), form).cpu().numpy().astype(np.float64)
+    emu, A = _emulate(m, g, form)
+    assert np.all(np.abs(got - emu) <= 2e-6 * A), np.max(np.abs(got - emu) / A)
+    exact = _fp64(m, g)
+    Ax = np.abs(16 * float(m.w0)) + np.abs(g.astype(np.float64)) @ np.abs(m.w_lin.astype(np.float64)) + \
+        np.einsum("ni,ij,nj->n", np.abs(g[:, :16].astype(np.float64)), np.abs(np.tril(m.w_quad.reshape(16, 16))),
+                  np.abs(g[:, :16].astype(np.float64)))
+    rel = np.abs(got - exact) / Ax
+    bound = 3 * 2.0 ** -8 if form == "bf16" else 3 * 2.0 ** -11
+    assert rel.max() <= bound, (rel.max(), bound)
+    # a padded row stride and a ragged tail
+    g2 = np.zeros((1000, 32), np.float32)
+    g2[:, :29] = g[:1000]
+    got2 = precision.tc_score(m, torch.from_numpy(g2).cuda(), form).cpu().numpy()
+    np.testing.assert_array_equal(got2, got[:1000].astype(np.float32))
