@@ -57,7 +57,7 @@ def parse():
     ap.add_argument("--keep", type=int, default=KEEP)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="generation", choices=["generation", "islands"],
+    ap.add_argument("--workload", default="generation", choices=["generation", "islands", "precision"],
                     help="islands: 20 islands batched in one graph launch (not the headline line)")
     ap.add_argument("--islands", type=int, default=20)
     return ap.parse_args()
@@ -265,8 +265,97 @@ def run_islands(args):
     print(json.dumps(line), flush=True)
 
 
+def _fp64_scores(model, g):
+    import numpy as np
+
+    g = np.asarray(g, dtype=np.float64)
+    L = np.tril(model.w_quad.astype(np.float64).reshape(16, 16))
+    return 16 * float(model.w0) + g @ model.w_lin.astype(np.float64) + np.einsum("ni,ij,nj->n", g[:, :16], L, g[:, :16])
+
+
+def run_precision(args):
+    """The precision form on the generation workload: BF16 and FP16 tensor-core
+    screens against the plain FP32 screen, with top-256 recall against the FP64
+    top-256 and score errors against FP64."""
+    import numpy as np
+    import torch
+
+    from codec_arena_gb300 import _lib, precision, screen, workloads as wl
+
+    torch.cuda.set_device(0)
+    el = wl.seeded_elites(N_ELITES)
+    model = screen.Model.from_compact(wl.surrogate_161())
+    d_el = torch.from_numpy(el.view(np.uint8).copy()).cuda()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    out = {}
+    sampler = ClockSampler(0)
+    sampler.start()
+    for name, flag in (("fp32_plain", 0), ("bf16_tc", _lib.FLAG_TC_BF16), ("fp16_tc", _lib.FLAG_TC_FP16)):
+        cfg = screen.Cfg(args.lam, args.keep, SEED, threads=args.threads, flags=flag | _lib.FLAG_STAGE_TIMES)
+        d_out = torch.zeros(args.keep * 168, dtype=torch.uint8, device="cuda")
+        d_res = torch.zeros(4, dtype=torch.int64, device="cuda")
+        for _ in range(max(3, args.warmup)):
+            screen.screen_device(cfg, model, d_el, d_out, d_res)
+        ms, kms = [], []
+        for _ in range(args.steps):
+            flush.fill_(1)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            screen.screen_device(cfg, model, d_el, d_out, d_res)
+            b.record()
+            b.synchronize()
+            ms.append(a.elapsed_time(b))
+            kms.append(screen.last_run_info()["ms_screen"])
+        res = d_res.cpu().numpy()
+        assert res[2] == 0 and res[1] == args.lam
+        surv = screen.survivors_from_bytes(d_out.cpu().numpy(), int(res[0]))
+        info = screen.last_run_info()
+        out[name] = {"value": args.lam / (statistics.mean(ms) / 1000), "ms_per_step": statistics.mean(ms),
+                     "screen_kernel_ms": statistics.mean(kms), "fp64_or_exact_rescored": info["exact_evals"],
+                     "screen_ctas": info["screen_ctas"], "_surv": surv}
+    clocks = sampler.stop()
+    # FP64 ground truth: the exact screen's top 4096, rescored in FP64 (certified below)
+    cfg = screen.Cfg(args.lam, 4096, SEED, threads=args.threads)
+    big, _ = screen.screen(cfg, model, el)
+    s64 = _fp64_scores(model, big["g"])
+    order = np.lexsort((big["index"], big["stream"], -s64))
+    K = args.keep
+    truth = {(int(big["stream"][i]), int(big["index"][i])) for i in order[:K]}
+    L = np.tril(model.w_quad.reshape(16, 16).astype(np.float64))
+    A = 16 * abs(float(model.w0)) + np.abs(model.w_lin).sum() + np.abs(L).sum()
+    e32 = 36 * 2.0 ** -24 * A  # exact-order FP32 error bound (gamma_35)
+    certified = bool(float(big["score"][-1]) + e32 < s64[order[K - 1]])
+    for name in out:
+        have = {(int(r["stream"]), int(r["index"])) for r in out[name].pop("_surv")}
+        out[name]["recall_top%d_vs_fp64" % K] = len(have & truth) / K
+    # score errors of the tensor-core forms against FP64
+    g_top = torch.from_numpy(np.ascontiguousarray(big["g"])).cuda()
+    rng = np.random.default_rng(5)
+    g_rand = torch.from_numpy(rng.random((1_000_000, 29), dtype=np.float32)).cuda()
+    s64_rand = _fp64_scores(model, g_rand.cpu().numpy())
+    errs = {}
+    for form in ("bf16", "fp16"):
+        e_top = np.abs(precision.tc_score(model, g_top, form).cpu().numpy() - s64)
+        e_rand = np.abs(precision.tc_score(model, g_rand, form).cpu().numpy() - s64_rand)
+        errs[form] = {"max_abs_top4096": float(e_top.max()), "mean_abs_top4096": float(e_top.mean()),
+                      "max_rel_top4096": float((e_top / np.abs(s64)).max()),
+                      "max_abs_uniform1e6": float(e_rand.max()), "mean_abs_uniform1e6": float(e_rand.mean())}
+        out[form + "_tc"]["score_error_vs_fp64"] = errs[form]
+    line = {"metric": "candidates/sec, 1 GB300: BF16-TC fused vs FP32 plain at top-256 recall>=0.999",
+            "value": out["bf16_tc"]["value"], "unit": "candidates/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": out["bf16_tc"]["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (tensor cores) + f64 band; genes u64/f32",
+            "data": "synthetic (seeded)", "config": workload_config(args, 1),
+            "forms": out, "bf16_over_fp32": out["bf16_tc"]["value"] / out["fp32_plain"]["value"],
+            "fp64_truth": {"from": "exact FP32 screen top-4096 rescored in FP64", "certified_complete": certified},
+            "clocks": clocks}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "precision" and args.impl != "reference":
+        return run_precision(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "islands":

@@ -31,6 +31,8 @@ FLAG_OUTPUT_29 = 0x2
 FLAG_PARSE_V6_FIX = 0x4
 FLAG_EXACT_ALL = 0x8
 FLAG_STAGE_TIMES = 0x10
+FLAG_TC_BF16 = 0x20
+FLAG_TC_FP16 = 0x40
 
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libcsx_screen.so")
 

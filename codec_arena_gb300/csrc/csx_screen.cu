@@ -946,6 +946,7 @@ struct Plan {
     size_t smem = 0;
     bool fast_delta = true;
     bool filter = false;
+    bool tc = false, fp16 = false;  // precision form (tensor cores + FP64 band)
     float err = 0.0f;
 };
 
@@ -969,12 +970,281 @@ ScreenFn screen_fn(bool fast_delta, bool filter) {
     return filter ? screen_kernel<false, true> : screen_kernel<false, false>;
 }
 
-int screen_occupancy(ScreenFn fn, int num_sms, size_t smem, int *blocks) {
+template <typename Fn>
+int screen_occupancy(Fn fn, int num_sms, size_t smem, int *blocks) {
     CSX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     int nb = 0;
     CSX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kThreads, smem));
     *blocks = std::max(1, nb) * num_sms;
     return CSX_OK;
+}
+
+// ---- precision form (tensor cores), used by make_plan / enqueue_screen -------------
+
+int make_tc_model(const csx_model &m, bool fp16, TcModel *t);
+
+constexpr float kTcBand = 1e-3f;  // relative band below the K-th score rescored in FP64
+constexpr size_t kTcSmemExtra = 1024 + 2 * 4096 + 512;  // alignment slack, two X tiles, the B tile
+
+struct TcScreenArgs {
+    ScreenArgs A;
+    TcModel tm;
+    float band;     // relative band below the threshold
+    float err_abs;  // certified bound on |tensor-core score - exact score|: the band is never narrower
+};
+
+int tc_error_bound(const csx_model &m, bool fp16, float *out);
+
+__device__ __forceinline__ double score64_genes(const DevModel &m, const float (&g)[kNtot]) {
+    double s = 16.0 * static_cast<double>(m.w0);
+#pragma unroll
+    for (int k = 0; k < kNtot; ++k) s = fma(static_cast<double>(m.wlin[k]), static_cast<double>(g[k]), s);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        double t = 0.0;
+#pragma unroll
+        for (int j = 0; j <= i; ++j) t = fma(static_cast<double>(m.wq[tri(i, j)]), static_cast<double>(g[j]), t);
+        s = fma(t, static_cast<double>(g[i]), s);
+    }
+    return s;
+}
+
+// FP64 score of the candidate at p (genes regenerated exactly), out of line.
+template <bool kFastDelta>
+__device__ __noinline__ double score64_at(const DevModel *m, const SynthConst *sc, const float *el, uint64_t seed_t,
+                                          uint64_t p) {
+    const CandHead h = cand_head(*sc, seed_t, p);
+    float g[kNtot];
+    (void)synth_score<kFastDelta, true, true>(*m, *sc, el, seed_t, p, h, g);
+    return score64_genes(*m, g);
+}
+
+// The screen in the precision form: the quadratic block of every candidate on
+// the tensor cores (two 128-thread groups, one MMA per group per round), the
+// FP64 score for candidates within `band` (relative) of the CTA threshold,
+// ranking by that FP64 score rounded to f32. Rounds are group-uniform: a
+// thread without work feeds a zero row.
+template <bool kFastDelta, bool kFp16>
+__global__ void __launch_bounds__(kThreads, 2) screen_tc_kernel(const __grid_constant__ TcScreenArgs P) {
+    const ScreenArgs &A = P.A;
+    extern __shared__ __align__(16) unsigned char smem_raw[];  // tiles are aligned by address below
+    Entry *E = reinterpret_cast<Entry *>(smem_raw);
+    float *el = reinterpret_cast<float *>(E + A.sort_n);
+    __shared__ __align__(8) unsigned long long s_mbar[2];
+    __shared__ uint32_t s_tbase;
+    __shared__ unsigned int s_buf_n;
+    __shared__ unsigned long long s_t1, s_t2;
+    __shared__ float s_ts;
+
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, grp = warp >> 2;
+    const uint32_t base = smem_u32(smem_raw);
+    const uint32_t after = base + A.sort_n * static_cast<uint32_t>(sizeof(Entry)) + (A.sc.ne + 1) * kNtot * 4u;
+    const uint32_t xs0 = (after + 1023u) & ~1023u;
+    const uint32_t bts = xs0 + 2u * 4096u;
+    for (uint32_t i = tid; i < A.sort_n; i += kThreads) E[i] = Entry{0ull, 0ull};
+    for (uint32_t i = tid; i < (A.sc.ne + 1) * kNtot; i += kThreads) el[i] = A.el[i];
+    for (uint32_t i = tid; i < 128; i += kThreads)
+        reinterpret_cast<uint32_t *>(smem_raw + (bts - base))[i] = reinterpret_cast<const uint32_t *>(P.tm.btile)[i];
+    if (warp == 0) tc_alloc(smem_u32(&s_tbase), 32);
+    if (tid == 0) {
+        mbar_init(smem_u32(&s_mbar[0]), 1);
+        mbar_init(smem_u32(&s_mbar[1]), 1);
+        s_buf_n = 0;
+        s_t1 = 0;
+        s_t2 = 0;
+        s_ts = -INFINITY;
+    }
+    const unsigned int n_items = *reinterpret_cast<volatile unsigned int *>(&A.ctrl->n_items);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    TcGroup tg;
+    tg.xs = xs0 + grp * 4096u;
+    tg.mbar = smem_u32(&s_mbar[grp]);
+    tg.tmem_d = s_tbase + 16u * grp;
+    tg.tmem_ld = s_tbase + ((32u * (warp & 3u)) << 16) + 16u * grp;
+    tg.adesc = tc_sdesc(tg.xs, 128, 256);
+    tg.bdesc = tc_sdesc(bts, 128, 256);
+    tg.idesc = tc_idesc(kFp16);
+    tg.bar_id = 1u + grp;
+    tg.phase = 0;
+    tg.issuer = (tid & 127u) == 0;
+    bool tc_ok = true;
+
+    Entry *buf = E + A.kpad;
+    uint32_t item = atomicAdd(&A.ctrl->next_item, 1u);
+    bool valid = item < n_items;
+    uint64_t seed_t = 0, p = 0;
+    uint32_t left = 0, dcand = 0, ddraw = 0;
+    if (valid) {
+        const Item it = A.items[item];
+        seed_t = stream_seed(A.seed, it.stream);
+        p = it.draw0;
+        left = it.n;
+        valid = left > 0;
+    }
+    unsigned long long screened = 0, exact = 0;
+    unsigned int gk = 0;
+    uint32_t round = 0;
+    bool has_def = false;
+    Entry def{0ull, 0ull};
+
+    for (;;) {
+        __syncthreads();
+        const unsigned int bn = s_buf_n;
+        const int any = __syncthreads_or(valid || has_def);
+        if (bn >= A.buf_cap / 2 || (!any && bn > 0)) {
+            cta_sort_desc(E, A.sort_n);
+            for (uint32_t i = A.kpad + tid; i < A.sort_n; i += kThreads) E[i] = Entry{0ull, 0ull};
+            if (tid == 0) {
+                s_buf_n = 0;
+                const Entry kth = E[A.keep - 1];
+                if (kth.k1 != 0ull) {
+                    s_t1 = kth.k1;
+                    s_t2 = kth.k2;
+                    const unsigned int ok = static_cast<unsigned int>(kth.k1 >> 32);
+                    s_ts = okey_score(ok);
+                    atomicMax(&A.ctrl->gtau, ok);
+                }
+            }
+            __syncthreads();
+        }
+        if (!any) break;
+        if (has_def) {
+            const unsigned int slot = atomicAdd(&s_buf_n, 1u);
+            buf[slot] = def;
+            has_def = false;
+        }
+        unsigned long long t1 = s_t1, t2 = s_t2;
+        float ts = s_ts;
+        if ((round++ & 7u) == 0) gk = *reinterpret_cast<volatile unsigned int *>(&A.ctrl->gtau);
+        if ((static_cast<unsigned long long>(gk) << 32) > t1) {
+            t1 = static_cast<unsigned long long>(gk) << 32;
+            t2 = 0;
+            ts = okey_score(gk);
+        }
+        const float tlo = __fsub_rd(ts, fmaxf(__fmul_ru(P.band, fabsf(ts)), P.err_abs));
+#pragma unroll 1
+        for (int r = 0; r < kRounds; ++r) {
+            const bool act = valid && !has_def;
+            float R = 0.0f, x[16];
+            uint32_t pk[8];
+            uint32_t len = 0;
+            if (act) {
+                const CandHead h = cand_head(A.sc, seed_t, p);
+                synth_tc<kFastDelta, kFp16>(P.tm, A.sc, el, seed_t, p, h, R, x, pk);
+                len = h.len;
+            } else {
+#pragma unroll
+                for (int j = 0; j < 8; ++j) pk[j] = 0u;
+#pragma unroll
+                for (int i = 0; i < 16; ++i) x[i] = 0.0f;
+            }
+            float y[16];
+            tc_ok = tc_round(tg, pk, tid & 127u, y) && tc_ok;
+            if (act) {
+                float s = R;
+#pragma unroll
+                for (int i = 0; i < 16; ++i) s = __fmaf_rn(x[i], y[i], s);
+                if (s >= tlo) {
+                    const float sf = static_cast<float>(score64_at<kFastDelta>(&A.m, &A.sc, el, seed_t, p));
+                    ++exact;
+                    if (sf >= ts) {
+                        const unsigned long long k1 = (static_cast<unsigned long long>(score_okey(sf)) << 32) |
+                                                      static_cast<unsigned int>(~item);
+                        const unsigned long long k2 = (static_cast<unsigned long long>(~dcand) << 32) | ddraw;
+                        if (k1 > t1 || (k1 == t1 && k2 > t2)) {
+                            const unsigned int slot = atomicAdd(&s_buf_n, 1u);
+                            if (slot < A.buf_cap) {
+                                buf[slot] = Entry{k1, k2};
+                            } else {
+                                has_def = true;
+                                def = Entry{k1, k2};
+                            }
+                        }
+                    }
+                }
+                p += len;
+                ddraw += len;
+                ++dcand;
+                ++screened;
+                if (--left == 0) {
+                    item = atomicAdd(&A.ctrl->next_item, 1u);
+                    valid = item < n_items;
+                    if (valid) {
+                        const Item it = A.items[item];
+                        seed_t = stream_seed(A.seed, it.stream);
+                        p = it.draw0;
+                        left = it.n;
+                        dcand = 0;
+                        ddraw = 0;
+                        valid = left > 0;
+                    }
+                }
+            }
+        }
+    }
+    Entry *out = A.lists + static_cast<size_t>(blockIdx.x) * A.kpad;
+    for (uint32_t i = tid; i < A.kpad; i += kThreads) out[i] = E[i];
+    for (int o = 16; o > 0; o >>= 1) {
+        screened += __shfl_down_sync(0xffffffffu, screened, o);
+        exact += __shfl_down_sync(0xffffffffu, exact, o);
+    }
+    if ((tid & 31) == 0) {
+        atomicAdd(&A.ctrl->screened, screened);
+        atomicAdd(&A.ctrl->exact_evals, exact);
+    }
+    if (!tc_ok) atomicOr(&A.ctrl->err, kErrTc);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tc_dealloc(s_tbase, 32);
+}
+
+using TcScreenFn = void (*)(TcScreenArgs);
+
+TcScreenFn screen_tc_fn(bool fast_delta, bool fp16) {
+    if (fast_delta) return fp16 ? screen_tc_kernel<true, true> : screen_tc_kernel<true, false>;
+    return fp16 ? screen_tc_kernel<false, true> : screen_tc_kernel<false, false>;
+}
+
+// Survivor regeneration for the precision form: the key holds the FP64 score
+// rounded to f32.
+template <bool kFastDelta>
+__global__ void regen64_kernel(const __grid_constant__ ScreenArgs A, const Entry *__restrict__ fin,
+                               const unsigned long long *__restrict__ ids, const unsigned int *__restrict__ tribes,
+                               csx_survivor *__restrict__ out) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= A.keep) return;
+    const Entry e = fin[q];
+    const bool real = e.k1 != 0ull;
+    const bool next_real = (q + 1 < A.keep) ? (fin[q + 1].k1 != 0ull) : false;
+    if (q == 0 && !real) A.ctrl->n_out = 0;
+    if (real && !next_real) A.ctrl->n_out = q + 1;
+    if (!real) return;
+    const uint32_t item = ~static_cast<uint32_t>(e.k1);
+    const uint32_t dcand = ~static_cast<uint32_t>(e.k2 >> 32);
+    const uint32_t ddraw = static_cast<uint32_t>(e.k2);
+    const Item it = A.items[item];
+    const uint64_t seed_t = stream_seed(A.seed, it.stream);
+    const uint64_t draw = it.draw0 + ddraw;
+    const CandHead h = cand_head(A.sc, seed_t, draw);
+    float genes[kNtot];
+    (void)synth_score<kFastDelta, true>(A.m, A.sc, A.el, seed_t, draw, h, genes);
+    const float s = static_cast<float>(score64_genes(A.m, genes));
+    if (score_okey(s) != static_cast<unsigned int>(e.k1 >> 32)) atomicOr(&A.ctrl->err, kErrRegen);
+    csx_survivor v;
+    v.score = s;
+    v.tribe = tribes[h.ea];
+    v.pa = ids[h.ea];
+    v.pb = ids[h.eb];
+    v.stream = it.stream;
+    v.index = it.idx0 + dcand;
+    v.draw = draw;
+#pragma unroll
+    for (int k = 0; k < kNtot; ++k) v.g[k] = genes[k];
+    v.reserved = 0;
+    out[q] = v;
 }
 
 // Bound on |filter score - exact score| for genes in [0, 1]: the exact
@@ -1015,11 +1285,18 @@ int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int
     pl->kpad = std::max<uint32_t>(32, pow2_at_least(cfg.keep));
     pl->sort_n = pow2_at_least(pl->kpad + 4ull * kThreads);
     pl->buf_cap = pl->sort_n - pl->kpad;
+    const uint32_t tcf = cfg.flags & (CSX_FLAG_TC_BF16 | CSX_FLAG_TC_FP16);
+    if (tcf == (CSX_FLAG_TC_BF16 | CSX_FLAG_TC_FP16)) return CSX_ERR_BAD_ARGS;
+    pl->tc = tcf != 0;
+    pl->fp16 = tcf == CSX_FLAG_TC_FP16;
     pl->smem = static_cast<size_t>(pl->sort_n) * sizeof(Entry) +
-               static_cast<size_t>(ne + 1) * kNtot * sizeof(float);
+               static_cast<size_t>(ne + 1) * kNtot * sizeof(float) + (pl->tc ? kTcSmemExtra : 0);
     if (pl->smem + 1024 > cx.max_smem) return CSX_ERR_LIMIT;
     if (grid_override > 0) {
         pl->grid = grid_override;
+    } else if (pl->tc) {
+        int rc = screen_occupancy(screen_tc_fn(pl->fast_delta, pl->fp16), cx.num_sms, pl->smem, &pl->grid);
+        if (rc) return rc;
     } else {
         int rc = screen_occupancy(screen_fn(pl->fast_delta, pl->filter), cx.num_sms, pl->smem, &pl->grid);
         if (rc) return rc;
@@ -1156,7 +1433,18 @@ int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, cons
     A.sort_n = pl.sort_n;
     A.buf_cap = pl.buf_cap;
     A.err = pl.err;
-    screen_fn(fast, pl.filter)<<<pl.grid, kThreads, pl.smem, st>>>(A);
+    if (pl.tc) {
+        TcScreenArgs P;
+        P.A = A;
+        P.band = kTcBand;
+        rc = make_tc_model(model, pl.fp16, &P.tm);
+        if (rc) return rc;
+        rc = tc_error_bound(model, pl.fp16, &P.err_abs);
+        if (rc) return rc;
+        screen_tc_fn(fast, pl.fp16)<<<pl.grid, kThreads, pl.smem, st>>>(P);
+    } else {
+        screen_fn(fast, pl.filter)<<<pl.grid, kThreads, pl.smem, st>>>(A);
+    }
     CSX_CUDA(cudaGetLastError());
     ++launches;
     CSX_CUDA(mark(3));
@@ -1176,7 +1464,11 @@ int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, cons
         n = m;
     }
     CSX_CUDA(mark(4));
-    if (fast)
+    if (pl.tc && fast)
+        regen64_kernel<true><<<unit_blocks(cfg.keep, 128), 128, 0, st>>>(A, cur, ids, tribes, d_out);
+    else if (pl.tc)
+        regen64_kernel<false><<<unit_blocks(cfg.keep, 128), 128, 0, st>>>(A, cur, ids, tribes, d_out);
+    else if (fast)
         regen_kernel<true><<<unit_blocks(cfg.keep, 128), 128, 0, st>>>(A, cur, ids, tribes, d_out, d_result);
     else
         regen_kernel<false><<<unit_blocks(cfg.keep, 128), 128, 0, st>>>(A, cur, ids, tribes, d_out, d_result);
@@ -1540,6 +1832,7 @@ extern "C" int csx_screen_device_noalloc(const csx_cfg *cfg, const csx_model *mo
                                          uint64_t out_cap, uint64_t *d_result, void *cuda_stream) {
     int rc = check_common(cfg, model, n_elites);
     if (rc) return rc;
+    if (cfg->flags & (CSX_FLAG_TC_BF16 | CSX_FLAG_TC_FP16)) return CSX_ERR_BAD_ARGS;  // csx_screen_device only
     if (!d_elites || !d_result || (!d_out && cfg->lambda > 0)) return CSX_ERR_BAD_ARGS;
     if (out_cap < std::min<uint64_t>(cfg->keep, cfg->lambda)) return CSX_ERR_BAD_ARGS;
     int count = 0, dev = 0;
@@ -2135,6 +2428,7 @@ int check_batch(int n, const csx_cfg *cfgs, const csx_model *models, const int *
     for (int i = 0; i < n; ++i) {
         int rc = check_common(&cfgs[i], &models[i], n_elites[i]);
         if (rc) return rc;
+        if (cfgs[i].flags & (CSX_FLAG_TC_BF16 | CSX_FLAG_TC_FP16)) return CSX_ERR_BAD_ARGS;  // single screens only
     }
     return CSX_OK;
 }
@@ -2341,6 +2635,40 @@ int make_tc_model(const csx_model &m, bool fp16, TcModel *t) {
             const int off = (n >> 3) * 256 + (k >> 3) * 128 + (n & 7) * 16 + (k & 7) * 2;
             t->btile[off / 2] = bits;
         }
+    return CSX_OK;
+}
+
+// Bound on |precision-form score - exact score| for genes in [0, 1]
+// (u = unit roundoff of the tile format, SL = sum |L_ij|, SL' = SL / 4):
+//   BF16: x = bf16(g), L rounded: (2u + u^2) SL, u = 2^-9;
+//   FP16: x' = fp16(fl(2g - 1)), L/4 rounded: (2u + u^2) SL' + 2^-25 (2 SL' + 136 * 2^-25)
+//         (subnormal spacing and the f32 rounding of 2g - 1), u = 2^-12,
+//         plus the f32 rounding of the folded constant and linear terms;
+// and for both the tensor-core accumulation (taken as 2^-18 relative, a
+// margin over FP32), the FP32 row dot (gamma_17) and the FP32 linear part
+// (gamma_31) on the absolute sums of their terms.
+int tc_error_bound(const csx_model &m, bool fp16, float *out) {
+    double SL = 0.0, lin = 16.0 * std::fabs(static_cast<double>(m.w0));
+    for (int i = 0; i < 16; ++i)
+        for (int j = 0; j <= i; ++j) SL += std::fabs(static_cast<double>(m.w_quad[i * 16 + j]));
+    for (int k = 0; k < kNtot; ++k) lin += std::fabs(static_cast<double>(m.w_lin[k]));
+    const double u24 = std::ldexp(1.0, -24);
+    auto gamma = [u24](double n) { return n * u24 / (1.0 - n * u24); };
+    double e;
+    if (!fp16) {
+        const double u = std::ldexp(1.0, -9);
+        e = (2 * u + u * u) * SL + (std::ldexp(1.0, -18) + gamma(17)) * SL * (1 + 4 * u) + gamma(31) * lin;
+    } else {
+        const double u = std::ldexp(1.0, -12), sl = SL / 4.0;
+        const double t25 = std::ldexp(1.0, -25);
+        // folded terms: |c''| + sum |lin''| <= lin + 7 sl (u_i sums to 2 sl, v to sl)
+        const double lin2 = lin + 7.0 * sl;
+        e = (2 * u + u * u) * sl + t25 * (2 * sl + 136 * t25) + (std::ldexp(1.0, -18) + gamma(17)) * sl * 1.01 +
+            (gamma(31) + u24) * lin2;
+    }
+    e = e * (1.0 + std::ldexp(1.0, -20)) + 1e-30;
+    if (!std::isfinite(e) || e > 1e30) return CSX_ERR_BAD_MODEL;
+    *out = std::nextafter(static_cast<float>(e), INFINITY);
     return CSX_OK;
 }
 

@@ -55,6 +55,12 @@ enum {
 #define CSX_FLAG_EXACT_ALL 0x8u    /* score every candidate in the reference's f32 order
                                       instead of filtering with a certified fast score */
 #define CSX_FLAG_STAGE_TIMES 0x10u /* record per-stage device times (csx_last_run_info) */
+#define CSX_FLAG_TC_BF16 0x20u     /* precision form: quadratic block on the tensor cores in BF16;
+                                      candidates within max(1e-3 relative, the form's certified
+                                      error bound) of the K-th score are rescored in FP64 and the
+                                      survivors ranked by that FP64 score (rounded to f32): the
+                                      FP64 top-K, genes bit-exact. csx_screen / csx_screen_device */
+#define CSX_FLAG_TC_FP16 0x40u     /* the same in FP16 with x' = 2g - 1 */
 
 /* Model: the flat weight layout of src/screen.zig:23-27. */
 typedef struct csx_model {

@@ -79,3 +79,62 @@ def test_tc_score_matches_emulation_and_bounds(form, which):
     g2[:, :29] = g[:1000]
     got2 = precision.tc_score(m, torch.from_numpy(g2).cuda(), form).cpu().numpy()
     np.testing.assert_array_equal(got2, got[:1000].astype(np.float32))
+
+
+def _truth(orc, w, el, lam, K, seed, T, sigma=0.12):
+    """Every candidate from the oracle, scored in FP64; the FP64 top-K by
+    (score desc, stream, index)."""
+    c = orc.cfg(lam, K, seed, threads=T, sigma=sigma)
+    m = orc.model_from_compact(w)
+    per = lam // T
+    cands = np.concatenate([orc.stream_dump(c, m, el, t, per if t < T - 1 else lam - (T - 1) * per)
+                            for t in range(T)])
+    from codec_arena_gb300 import screen
+
+    s64 = _fp64(screen.Model.from_compact(w), cands["g"])
+    order = np.lexsort((cands["index"], cands["stream"], -s64))
+    return cands, s64, order
+
+
+@pytest.mark.parametrize("form,which", [("bf16", "v3"), ("fp16", "v3"), ("bf16", "normal"), ("fp16", "normal")])
+def test_tc_screen_is_fp64_top_k(orc, form, which):
+    """The precision screen returns the FP64 top-K: its band (max of 1e-3
+    relative and the form's certified error bound) never drops a candidate of
+    the FP64 top-K. Genes and lineage are bit-exact; scores are the FP64 score
+    rounded to f32."""
+    from codec_arena_gb300 import _lib, screen, workloads as wl
+
+    w = wl.surrogate_161() if which == "v3" else wl.seeded_normal_model(seed=2)
+    el = wl.seeded_elites(64)
+    lam, K, T, seed = 600_000, 256, 4, 7
+    flag = _lib.FLAG_TC_BF16 if form == "bf16" else _lib.FLAG_TC_FP16
+    got, n = screen.screen(screen.Cfg(lam, K, seed, threads=T, flags=flag), screen.Model.from_compact(w), el)
+    assert n == lam and len(got) == K
+    cands, s64, order = _truth(orc, w, el, lam, K, seed, T)
+    pos = {(int(cands["stream"][i]), int(cands["index"][i])): i for i in order[: 4 * K]}
+    for r in got:
+        i = pos[(int(r["stream"]), int(r["index"]))]
+        assert r["g"].tobytes() == cands["g"][i].tobytes()
+        assert (r["pa"], r["pb"], r["tribe"], r["draw"]) == (cands["pa"][i], cands["pb"][i], cands["tribe"][i],
+                                                               cands["draw"][i])
+        assert abs(float(r["score"]) - s64[i]) <= abs(s64[i]) * 2 ** -23
+    want = {(int(cands["stream"][i]), int(cands["index"][i])) for i in order[:K]}
+    have = {(int(r["stream"]), int(r["index"])) for r in got}
+    # ties at f32 resolution of the K-th FP64 score may swap members; otherwise the sets agree
+    kth = np.float32(s64[order[K - 1]])
+    diff = (want ^ have)
+    assert all(np.float32(s64[pos[k]] if k in pos else -np.inf) == kth for k in diff), len(diff)
+    scores = got["score"]
+    assert np.all(scores[:-1] >= scores[1:])
+
+
+def test_tc_screen_deterministic_and_counts():
+    from codec_arena_gb300 import _lib, screen, workloads as wl
+
+    w = wl.surrogate_161()
+    el = wl.seeded_elites(64)
+    cfg = screen.Cfg(3_000_000, 128, 11, threads=4, flags=_lib.FLAG_TC_FP16)
+    a, na = screen.screen(cfg, screen.Model.from_compact(w), el)
+    b, nb = screen.screen(cfg, screen.Model.from_compact(w), el)
+    assert na == nb == 3_000_000
+    assert a.tobytes() == b.tobytes()
