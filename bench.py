@@ -14,6 +14,15 @@ T = 4 splitmix64 streams (the reference CI's --threads), sigma 0.12, jump
          integer-issue rates of this GPU (the path is integer-issue bound)
   cpu_baseline  the C restatement of the Zig screen (oracle/) on this host's
          cores, T = 4 as the reference CI, on a bounded prefix sample
+  precision_forms  the same generation with the quadratic block on the tensor
+         cores (BF16, and FP16 with x' = 2g - 1): throughput beside the plain
+         FP32 value, top-256 recall against the FP64 top-256, score errors
+
+The metric names the BF16 tensor-core form against the plain FP32 form; the
+line's value is the plain FP32 fused screen (the reference's own f32
+semantics, bit-exact), and precision_forms carries the BF16 / FP16 values.
+`--workload precision` prints a line whose value is the BF16 form;
+`--workload islands` the batched-islands workload.
 
 `--impl reference` times the reference's CPU implementation of the path (the
 restatement: Zig is not available) on the same workload, rank 0 only.
@@ -57,6 +66,7 @@ def parse():
     ap.add_argument("--keep", type=int, default=KEEP)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-precision", action="store_true", help="skip the tensor-core precision forms")
     ap.add_argument("--workload", default="generation", choices=["generation", "islands", "precision"],
                     help="islands: 20 islands batched in one graph launch (not the headline line)")
     ap.add_argument("--islands", type=int, default=20)
@@ -273,24 +283,27 @@ def _fp64_scores(model, g):
     return 16 * float(model.w0) + g @ model.w_lin.astype(np.float64) + np.einsum("ni,ij,nj->n", g[:, :16], L, g[:, :16])
 
 
-def run_precision(args):
-    """The precision form on the generation workload: BF16 and FP16 tensor-core
-    screens against the plain FP32 screen, with top-256 recall against the FP64
-    top-256 and score errors against FP64."""
+METRIC = "candidates/sec, 1 GB300: BF16-TC fused vs FP32 plain at top-256 recall>=0.999"
+
+
+def precision_forms(args, fp32_surv=None):
+    """BF16 and FP16 tensor-core screens of the generation workload beside the
+    plain FP32 screen: throughput (CUDA events, L2 flushed), top-K recall
+    against the FP64 top-K, and score errors against FP64."""
     import numpy as np
     import torch
 
     from codec_arena_gb300 import _lib, precision, screen, workloads as wl
 
-    torch.cuda.set_device(0)
     el = wl.seeded_elites(N_ELITES)
     model = screen.Model.from_compact(wl.surrogate_161())
     d_el = torch.from_numpy(el.view(np.uint8).copy()).cuda()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     out = {}
-    sampler = ClockSampler(0)
-    sampler.start()
-    for name, flag in (("fp32_plain", 0), ("bf16_tc", _lib.FLAG_TC_BF16), ("fp16_tc", _lib.FLAG_TC_FP16)):
+    forms = (("bf16_tc", _lib.FLAG_TC_BF16), ("fp16_tc", _lib.FLAG_TC_FP16))
+    if fp32_surv is None:
+        forms = (("fp32_plain", 0),) + forms
+    for name, flag in forms:
         cfg = screen.Cfg(args.lam, args.keep, SEED, threads=args.threads, flags=flag | _lib.FLAG_STAGE_TIMES)
         d_out = torch.zeros(args.keep * 168, dtype=torch.uint8, device="cuda")
         d_res = torch.zeros(4, dtype=torch.int64, device="cuda")
@@ -308,47 +321,59 @@ def run_precision(args):
             kms.append(screen.last_run_info()["ms_screen"])
         res = d_res.cpu().numpy()
         assert res[2] == 0 and res[1] == args.lam
-        surv = screen.survivors_from_bytes(d_out.cpu().numpy(), int(res[0]))
         info = screen.last_run_info()
         out[name] = {"value": args.lam / (statistics.mean(ms) / 1000), "ms_per_step": statistics.mean(ms),
-                     "screen_kernel_ms": statistics.mean(kms), "fp64_or_exact_rescored": info["exact_evals"],
-                     "screen_ctas": info["screen_ctas"], "_surv": surv}
-    clocks = sampler.stop()
-    # FP64 ground truth: the exact screen's top 4096, rescored in FP64 (certified below)
-    cfg = screen.Cfg(args.lam, 4096, SEED, threads=args.threads)
-    big, _ = screen.screen(cfg, model, el)
+                     "screen_kernel_ms": statistics.mean(kms), "rescored": info["exact_evals"],
+                     "screen_ctas": info["screen_ctas"],
+                     "_surv": screen.survivors_from_bytes(d_out.cpu().numpy(), int(res[0]))}
+    if fp32_surv is not None:
+        out["fp32_plain"] = {"_surv": fp32_surv}
+    # FP64 ground truth: the exact screen's top 4096 rescored in FP64, certified complete below
+    big, _ = screen.screen(screen.Cfg(args.lam, 4096, SEED, threads=args.threads), model, el)
     s64 = _fp64_scores(model, big["g"])
     order = np.lexsort((big["index"], big["stream"], -s64))
     K = args.keep
     truth = {(int(big["stream"][i]), int(big["index"][i])) for i in order[:K]}
     L = np.tril(model.w_quad.reshape(16, 16).astype(np.float64))
     A = 16 * abs(float(model.w0)) + np.abs(model.w_lin).sum() + np.abs(L).sum()
-    e32 = 36 * 2.0 ** -24 * A  # exact-order FP32 error bound (gamma_35)
+    e32 = 36 * 2.0 ** -24 * A  # the exact order's FP32 error bound (gamma_35 of the absolute terms)
     certified = bool(float(big["score"][-1]) + e32 < s64[order[K - 1]])
     for name in out:
         have = {(int(r["stream"]), int(r["index"])) for r in out[name].pop("_surv")}
-        out[name]["recall_top%d_vs_fp64" % K] = len(have & truth) / K
-    # score errors of the tensor-core forms against FP64
+        out[name]["recall_vs_fp64"] = len(have & truth) / K
     g_top = torch.from_numpy(np.ascontiguousarray(big["g"])).cuda()
     rng = np.random.default_rng(5)
-    g_rand = torch.from_numpy(rng.random((1_000_000, 29), dtype=np.float32)).cuda()
-    s64_rand = _fp64_scores(model, g_rand.cpu().numpy())
-    errs = {}
+    g_rand = rng.random((1_000_000, 29), dtype=np.float32)
+    s64_rand = _fp64_scores(model, g_rand)
+    g_rand = torch.from_numpy(g_rand).cuda()
     for form in ("bf16", "fp16"):
         e_top = np.abs(precision.tc_score(model, g_top, form).cpu().numpy() - s64)
         e_rand = np.abs(precision.tc_score(model, g_rand, form).cpu().numpy() - s64_rand)
-        errs[form] = {"max_abs_top4096": float(e_top.max()), "mean_abs_top4096": float(e_top.mean()),
-                      "max_rel_top4096": float((e_top / np.abs(s64)).max()),
-                      "max_abs_uniform1e6": float(e_rand.max()), "mean_abs_uniform1e6": float(e_rand.mean())}
-        out[form + "_tc"]["score_error_vs_fp64"] = errs[form]
-    line = {"metric": "candidates/sec, 1 GB300: BF16-TC fused vs FP32 plain at top-256 recall>=0.999",
-            "value": out["bf16_tc"]["value"], "unit": "candidates/s", "n_gpus": 1, "steps": args.steps,
-            "warmup": max(3, args.warmup), "ms_per_step": out["bf16_tc"]["ms_per_step"], "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (tensor cores) + f64 band; genes u64/f32",
-            "data": "synthetic (seeded)", "config": workload_config(args, 1),
-            "forms": out, "bf16_over_fp32": out["bf16_tc"]["value"] / out["fp32_plain"]["value"],
-            "fp64_truth": {"from": "exact FP32 screen top-4096 rescored in FP64", "certified_complete": certified},
+        out[form + "_tc"]["score_error_vs_fp64"] = {
+            "max_abs_top4096": float(e_top.max()), "mean_abs_top4096": float(e_top.mean()),
+            "max_rel_top4096": float((e_top / np.abs(s64)).max()),
+            "max_abs_uniform1e6": float(e_rand.max()), "mean_abs_uniform1e6": float(e_rand.mean())}
+    return {"forms": out, "fp64_truth": {"from": "exact FP32 screen top-4096 rescored in FP64",
+                                         "certified_complete": certified}}
+
+
+def run_precision(args):
+    """`--workload precision`: the BF16 tensor-core form as the line's value."""
+    import torch
+
+    torch.cuda.set_device(0)
+    sampler = ClockSampler(0)
+    sampler.start()
+    p = precision_forms(args)
+    clocks = sampler.stop()
+    f = p["forms"]
+    line = {"metric": METRIC, "value": f["bf16_tc"]["value"], "unit": "candidates/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": f["bf16_tc"]["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16 tensor cores + f64 band; genes u64/f32", "data": "synthetic (seeded)",
+            "config": workload_config(args, 1), "bf16_over_fp32": f["bf16_tc"]["value"] / f["fp32_plain"]["value"],
             "clocks": clocks}
+    line.update(p)
     print(json.dumps(line), flush=True)
 
 
@@ -471,7 +496,7 @@ def main():
         "issue_rates_measured": rates,
         "kernel_ms_per_launch": ms_screen,
     }
-    line = {"metric": "candidates/sec (screen generation, 1 GB300)", "value": value, "unit": "candidates/s",
+    line = {"metric": METRIC, "value": value, "unit": "candidates/s",
             "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
             "ms_per_step": 1000.0 * t_dev / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u64/f32", "data": "synthetic (seeded)",
@@ -482,6 +507,13 @@ def main():
                           items=int(res[3])),
             "exact_evals_last_step": stage[-1]["exact_evals"],
             "wall_s": wall}
+    if world == 1 and not args.no_precision:
+        # the BF16 / FP16 tensor-core forms of the same generation, beside this plain FP32 value
+        line["precision_forms"] = precision_forms(
+            args, fp32_surv=screen.survivors_from_bytes(d_out.cpu().numpy(), int(d_res[0].item())))
+        f = line["precision_forms"]["forms"]
+        f["fp32_plain"].update({"value": value, "ms_per_step": line["ms_per_step"]})
+        line["bf16_over_fp32"] = f["bf16_tc"]["value"] / value
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args, args.cpu_seconds)
     print(json.dumps(line), flush=True)

@@ -984,6 +984,7 @@ int screen_occupancy(Fn fn, int num_sms, size_t smem, int *blocks) {
 int make_tc_model(const csx_model &m, bool fp16, TcModel *t);
 
 constexpr float kTcBand = 1e-3f;  // relative band below the K-th score rescored in FP64
+constexpr int kTcCtasPerSm = 3;   // precision-form screen CTAs per SM
 constexpr size_t kTcSmemExtra = 1024 + 2 * 4096 + 512;  // alignment slack, two X tiles, the B tile
 
 struct TcScreenArgs {
@@ -1025,7 +1026,7 @@ __device__ __noinline__ double score64_at(const DevModel *m, const SynthConst *s
 // ranking by that FP64 score rounded to f32. Rounds are group-uniform: a
 // thread without work feeds a zero row.
 template <bool kFastDelta, bool kFp16>
-__global__ void __launch_bounds__(kThreads, 2) screen_tc_kernel(const __grid_constant__ TcScreenArgs P) {
+__global__ void __launch_bounds__(kThreads, 3) screen_tc_kernel(const __grid_constant__ TcScreenArgs P) {
     const ScreenArgs &A = P.A;
     extern __shared__ __align__(16) unsigned char smem_raw[];  // tiles are aligned by address below
     Entry *E = reinterpret_cast<Entry *>(smem_raw);
@@ -1295,8 +1296,13 @@ int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int
     if (grid_override > 0) {
         pl->grid = grid_override;
     } else if (pl->tc) {
+        // The occupancy query reports one CTA per SM for this kernel, yet three
+        // are resident and run faster (80 registers, ~50 KB of shared memory,
+        // 32 TMEM columns each; measured). The screen is persistent with
+        // dynamic work, so any grid is correct: launch three per SM.
         int rc = screen_occupancy(screen_tc_fn(pl->fast_delta, pl->fp16), cx.num_sms, pl->smem, &pl->grid);
         if (rc) return rc;
+        pl->grid = kTcCtasPerSm * cx.num_sms;
     } else {
         int rc = screen_occupancy(screen_fn(pl->fast_delta, pl->filter), cx.num_sms, pl->smem, &pl->grid);
         if (rc) return rc;

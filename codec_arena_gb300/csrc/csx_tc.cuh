@@ -153,7 +153,12 @@ __device__ __forceinline__ bool tc_round(TcGroup &g, const uint32_t (&pk)[8], ui
                  : "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     tc_fence_before();
-    asm volatile("bar.sync %0, 128;" ::"r"(g.bar_id) : "memory");
+    // literal barrier ids: a register id makes ptxas reserve all 16 named barriers,
+    // which limits how many CTAs an SM holds
+    if (g.bar_id == 1)
+        asm volatile("bar.sync 1, 128;" ::: "memory");
+    else
+        asm volatile("bar.sync 2, 128;" ::: "memory");
     if (g.issuer) {
         tc_fence_after();
         tc_mma(g.tmem_d, g.adesc, g.bdesc, g.idesc);
