@@ -22,7 +22,8 @@ The metric names the BF16 tensor-core form against the plain FP32 form; the
 line's value is the plain FP32 fused screen (the reference's own f32
 semantics, bit-exact), and precision_forms carries the BF16 / FP16 values.
 `--workload precision` prints a line whose value is the BF16 form;
-`--workload islands` the batched-islands workload.
+`--workload islands` the batched-islands workload, `--workload refit` the
+GPU ridge refit and the surrogate's forward / backward kernels.
 
 `--impl reference` times the reference's CPU implementation of the path (the
 restatement: Zig is not available) on the same workload, rank 0 only.
@@ -67,7 +68,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-precision", action="store_true", help="skip the tensor-core precision forms")
-    ap.add_argument("--workload", default="generation", choices=["generation", "islands", "precision"],
+    ap.add_argument("--workload", default="generation", choices=["generation", "islands", "precision", "refit"],
                     help="islands: 20 islands batched in one graph launch (not the headline line)")
     ap.add_argument("--islands", type=int, default=20)
     return ap.parse_args()
@@ -377,8 +378,85 @@ def run_precision(args):
     print(json.dumps(line), flush=True)
 
 
+def run_refit(args):
+    """Differentiable refit: ridge refit (alpha 1e-2) of 400,000 rows x 16 genes
+    (seeded quadratic truth + Student-t(3) noise) on the GPU -- FP64 normal
+    equations and FP64 Cholesky -- beside the reference's own numpy FP64 refit
+    (brain/evolve.py:259-265) on the host cores; the surrogate's forward and
+    backward kernels over the same rows."""
+    import numpy as np
+    import torch
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import refit as orc_refit
+
+    from codec_arena_gb300 import build, surrogate, workloads as wl
+
+    torch.cuda.set_device(0)
+    genes, fit, w_true = wl.refit_table()
+    n, nf, alpha = genes.shape[0], 153, 1e-2
+    d_g, d_y = torch.from_numpy(genes).cuda(), torch.from_numpy(fit).cuda()
+    prior = torch.zeros(nf, dtype=torch.float64, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def timed(fn):
+        out = []
+        for _ in range(max(3, args.warmup)):
+            fn()
+        for _ in range(args.steps):
+            flush.fill_(1)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            b.synchronize()
+            out.append(a.elapsed_time(b))
+        return statistics.mean(out)
+
+    sampler = ClockSampler(0)
+    sampler.start()
+    ms_refit = timed(lambda: surrogate.refit(d_g, d_y, prior, alpha))
+    ms_gram = timed(lambda: surrogate.normal_equations(d_g, d_y, nf))
+    G, r = surrogate.normal_equations(d_g, d_y, nf)
+    ms_solve = timed(lambda: surrogate.ridge_solve(G, r, alpha, prior))
+    coef = torch.from_numpy(w_true.astype(np.float32)).cuda().requires_grad_(True)
+    gg = d_g.clone().requires_grad_(True)
+    ms_fwd = timed(lambda: surrogate.score(d_g, coef.detach()))
+    ms_fwd_bwd = timed(lambda: surrogate.score(gg, coef).sum().backward())
+    clocks = sampler.stop()
+    w = surrogate.refit(d_g, d_y, prior, alpha).cpu().numpy()
+    # the reference's refit on the host (numpy FP64)
+    t0 = time.perf_counter()
+    w_np = orc_refit.refit_solve(genes, fit, np.zeros(nf), alpha)
+    cpu_s = time.perf_counter() - t0
+    bench = ctypes.CDLL(build.BENCH_LIB)
+    bench.csx_bench_issue_rate.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    dfma = ctypes.c_double(0)
+    bench.csx_bench_issue_rate(4, ctypes.byref(dfma))
+    gram_flop = 2.0 * n * (nf * (nf + 1) / 2 + nf)  # upper triangle + right-hand side, FP64
+    line = {"metric": "ridge refit time (400,000 rows x 16 genes, alpha 1e-2, FP64), 1 GB300", "value": ms_refit,
+            "unit": "ms", "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms_refit,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64 (normal equations, "
+            "Cholesky); f32 genes", "data": "synthetic (seeded quadratic truth + 0.5 * Student-t(3) noise)",
+            "config": {"workload": "ridge refit toward a zero prior: 400,000 rows of 16 genes, 153 features, alpha 1e-2",
+                       "rows": n, "features": nf, "alpha": alpha, "l2": "flushed between steps (256 MiB write)"},
+            "stages_ms": {"normal_equations": ms_gram, "cholesky_solve": ms_solve},
+            "roofline": {"bound": "fp64", "kernel": "sg_gram_kernel", "achieved": gram_flop / (ms_gram * 1e-3) / 1e12,
+                         "peak": 2 * dfma.value / 1e12, "unit": "TFLOP/s",
+                         "frac": gram_flop / (ms_gram * 1e-3) / (2 * dfma.value) if dfma.value else None,
+                         "peak_source": "measured: DFMA issue rate of this GPU (csx_bench_issue_rate kind 4)"},
+            "vs_numpy_fp64": {"max_abs_diff": float(np.abs(w - w_np).max()), "max_abs_w": float(np.abs(w_np).max()),
+                              "numpy_seconds": cpu_s, "host_threads": os.cpu_count(),
+                              "speedup": cpu_s * 1000 / ms_refit},
+            "surrogate_rows_per_s": {"forward": n / (ms_fwd * 1e-3), "forward_backward": n / (ms_fwd_bwd * 1e-3)},
+            "clocks": clocks, "gpu_launches": 4 * args.steps}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "refit" and args.impl != "reference":
+        return run_refit(args)
     if args.workload == "precision" and args.impl != "reference":
         return run_precision(args)
     if args.impl == "reference":

@@ -6,6 +6,7 @@
 //   kind 1  IMAD chain                                 -> lane-ops / s
 //   kind 2  FFMA chain                                 -> lane-ops / s
 //   kind 3  splitmix64 outputs (full 64-bit mixer)     -> hashes / s
+//   kind 4  DFMA chain (FP64 fused multiply-add)       -> lane-ops / s
 // Each thread runs 8 independent chains so issue, not latency, is measured.
 #include <cuda_runtime.h>
 
@@ -60,6 +61,20 @@ __global__ void ffma_kernel(uint32_t *out, int iters, float seed) {
     if (x == 1234.5f) out[0] = 1;
 }
 
+__global__ void dfma_kernel(uint32_t *out, int iters, double seed) {
+    double a[kChains];
+#pragma unroll
+    for (int j = 0; j < kChains; ++j) a[j] = seed + threadIdx.x * 1e-9 + j;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int j = 0; j < kChains; ++j) a[j] = fma(a[j], 0.9999999999, 1e-9);  // DFMA
+    }
+    double x = 0;
+#pragma unroll
+    for (int j = 0; j < kChains; ++j) x += a[j];
+    if (x == 1234.5) out[0] = 1;
+}
+
 __global__ void hash_kernel(uint32_t *out, int iters, uint64_t seed) {
     uint64_t s[kChains];
     uint64_t acc = 0;
@@ -81,14 +96,14 @@ __global__ void hash_kernel(uint32_t *out, int iters, uint64_t seed) {
 }  // namespace
 
 extern "C" int csx_bench_issue_rate(int kind, double *per_second) {
-    if (!per_second || kind < 0 || kind > 3) return -3;
+    if (!per_second || kind < 0 || kind > 4) return -3;
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return -8;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     uint32_t *out = nullptr;
     if (cudaMalloc(&out, 16) != cudaSuccess) return -9;
     const int threads = 256, blocks = sms * 8;
-    const int iters = kind == 3 ? 2000 : 20000;
+    const int iters = kind >= 3 ? 2000 : 20000;
     cudaEvent_t a, b;
     cudaEventCreate(&a);
     cudaEventCreate(&b);
@@ -99,6 +114,7 @@ extern "C" int csx_bench_issue_rate(int kind, double *per_second) {
             case 0: alu_kernel<<<blocks, threads>>>(out, iters, rep); break;
             case 1: imad_kernel<<<blocks, threads>>>(out, iters, rep); break;
             case 2: ffma_kernel<<<blocks, threads>>>(out, iters, 1.0f + rep); break;
+            case 4: dfma_kernel<<<blocks, threads>>>(out, iters, 1.0 + rep); break;
             default: hash_kernel<<<blocks, threads>>>(out, iters, rep); break;
         }
         cudaEventRecord(b);
@@ -115,7 +131,7 @@ extern "C" int csx_bench_issue_rate(int kind, double *per_second) {
         std::fprintf(stderr, "csx_bench: %s\n", cudaGetErrorString(e));
         return -7;
     }
-    const double ops_per_iter = kind == 0 ? 3.0 : 1.0;  // lane-ops (kinds 0-2) or hashes (3)
+    const double ops_per_iter = kind == 0 ? 3.0 : 1.0;  // lane-ops (kinds 0-2, 4) or hashes (3)
     *per_second = static_cast<double>(blocks) * threads * iters * kChains * ops_per_iter / (best * 1e-3);
     return 0;
 }

@@ -12,7 +12,8 @@ extern "C" {
 #endif
 
 /* kind 0: integer ALU (shift/xor/add) lane-ops/s; 1: IMAD lane-ops/s;
- * 2: FFMA lane-ops/s; 3: splitmix64 outputs/s. Returns 0 or a negative
+ * 2: FFMA lane-ops/s; 3: splitmix64 outputs/s; 4: DFMA (FP64) lane-ops/s
+ * (the ridge refit's normal equations). Returns 0 or a negative
  * csx status. Runs on the current device, default stream, synchronously. */
 int csx_bench_issue_rate(int kind, double *per_second);
 
