@@ -985,7 +985,7 @@ int make_tc_model(const csx_model &m, bool fp16, TcModel *t);
 
 constexpr float kTcBand = 1e-3f;  // relative band below the K-th score rescored in FP64
 constexpr int kTcCtasPerSm = 3;   // precision-form screen CTAs per SM
-constexpr size_t kTcSmemExtra = 1024 + 2 * 4096 + 512;  // alignment slack, two X tiles, the B tile
+constexpr size_t kTcSmemExtra = 512 * 12 + 1024 + 2 * 4096 + 512;  // band queue, alignment slack, two X tiles, B tile
 
 struct TcScreenArgs {
     ScreenArgs A;
@@ -1020,26 +1020,35 @@ __device__ __noinline__ double score64_at(const DevModel *m, const SynthConst *s
     return score64_genes(*m, g);
 }
 
+// A candidate waiting for its FP64 score (item-local index, draw offset).
+struct Pend {
+    uint32_t item, dcand, ddraw;
+};
+constexpr uint32_t kPendCap = 512;  // band queue per CTA
+
 // The screen in the precision form: the quadratic block of every candidate on
-// the tensor cores (two 128-thread groups, one MMA per group per round), the
-// FP64 score for candidates within `band` (relative) of the CTA threshold,
-// ranking by that FP64 score rounded to f32. Rounds are group-uniform: a
-// thread without work feeds a zero row.
+// the tensor cores (two 128-thread groups, one MMA per group per round).
+// Candidates whose tensor-core score is within the band of the CTA threshold
+// go to a shared queue; at the next merge all threads score the queue in FP64
+// (whole warps, not one lane per warp) and the results enter the top-K, ranked
+// by the FP64 score rounded to f32. Rounds are group-uniform: a thread without
+// work feeds a zero row.
 template <bool kFastDelta, bool kFp16>
 __global__ void __launch_bounds__(kThreads, 3) screen_tc_kernel(const __grid_constant__ TcScreenArgs P) {
     const ScreenArgs &A = P.A;
     extern __shared__ __align__(16) unsigned char smem_raw[];  // tiles are aligned by address below
     Entry *E = reinterpret_cast<Entry *>(smem_raw);
     float *el = reinterpret_cast<float *>(E + A.sort_n);
+    Pend *pend = reinterpret_cast<Pend *>(el + (A.sc.ne + 1) * kNtot);
     __shared__ __align__(8) unsigned long long s_mbar[2];
     __shared__ uint32_t s_tbase;
-    __shared__ unsigned int s_buf_n;
+    __shared__ unsigned int s_buf_n, s_pend_n;
     __shared__ unsigned long long s_t1, s_t2;
     __shared__ float s_ts;
 
     const uint32_t tid = threadIdx.x, warp = tid >> 5, grp = warp >> 2;
     const uint32_t base = smem_u32(smem_raw);
-    const uint32_t after = base + A.sort_n * static_cast<uint32_t>(sizeof(Entry)) + (A.sc.ne + 1) * kNtot * 4u;
+    const uint32_t after = smem_u32(pend + kPendCap);
     const uint32_t xs0 = (after + 1023u) & ~1023u;
     const uint32_t bts = xs0 + 2u * 4096u;
     for (uint32_t i = tid; i < A.sort_n; i += kThreads) E[i] = Entry{0ull, 0ull};
@@ -1051,6 +1060,7 @@ __global__ void __launch_bounds__(kThreads, 3) screen_tc_kernel(const __grid_con
         mbar_init(smem_u32(&s_mbar[0]), 1);
         mbar_init(smem_u32(&s_mbar[1]), 1);
         s_buf_n = 0;
+        s_pend_n = 0;
         s_t1 = 0;
         s_t2 = 0;
         s_ts = -INFINITY;
@@ -1087,41 +1097,68 @@ __global__ void __launch_bounds__(kThreads, 3) screen_tc_kernel(const __grid_con
     unsigned long long screened = 0, exact = 0;
     unsigned int gk = 0;
     uint32_t round = 0;
-    bool has_def = false;
-    Entry def{0ull, 0ull};
+    bool has_def = false;  // holds a band candidate the full queue could not take
+    Pend def{0u, 0u, 0u};
+
+    // FP64 score of a queued candidate; enters the buffer if it beats the threshold.
+    auto rescore = [&](const Pend &q, unsigned long long t1, unsigned long long t2, float ts) {
+        const Item it = A.items[q.item];
+        const uint64_t st = stream_seed(A.seed, it.stream);
+        const float sf = static_cast<float>(score64_at<kFastDelta>(&A.m, &A.sc, el, st, it.draw0 + q.ddraw));
+        ++exact;
+        if (sf >= ts) {
+            const unsigned long long k1 =
+                (static_cast<unsigned long long>(score_okey(sf)) << 32) | static_cast<unsigned int>(~q.item);
+            const unsigned long long k2 = (static_cast<unsigned long long>(~q.dcand) << 32) | q.ddraw;
+            if (k1 > t1 || (k1 == t1 && k2 > t2)) buf[atomicAdd(&s_buf_n, 1u)] = Entry{k1, k2};
+        }
+    };
 
     for (;;) {
         __syncthreads();
-        const unsigned int bn = s_buf_n;
+        const unsigned int pn = min(s_pend_n, kPendCap);
         const int any = __syncthreads_or(valid || has_def);
-        if (bn >= A.buf_cap / 2 || (!any && bn > 0)) {
-            cta_sort_desc(E, A.sort_n);
-            for (uint32_t i = A.kpad + tid; i < A.sort_n; i += kThreads) E[i] = Entry{0ull, 0ull};
-            if (tid == 0) {
-                s_buf_n = 0;
-                const Entry kth = E[A.keep - 1];
-                if (kth.k1 != 0ull) {
-                    s_t1 = kth.k1;
-                    s_t2 = kth.k2;
-                    const unsigned int ok = static_cast<unsigned int>(kth.k1 >> 32);
-                    s_ts = okey_score(ok);
-                    atomicMax(&A.ctrl->gtau, ok);
+        const int any_def = __syncthreads_or(has_def);
+        if (pn > 0 || any_def) {
+            // the buffer is empty here (it only fills from the queue, and every fill is sorted below)
+            unsigned long long t1 = s_t1, t2 = s_t2;
+            float ts = s_ts;
+            const unsigned int g = *reinterpret_cast<volatile unsigned int *>(&A.ctrl->gtau);
+            if ((static_cast<unsigned long long>(g) << 32) > t1) {
+                t1 = static_cast<unsigned long long>(g) << 32;
+                t2 = 0;
+                ts = okey_score(g);
+            }
+            for (uint32_t i = tid; i < pn; i += kThreads) rescore(pend[i], t1, t2, ts);
+            if (has_def) {
+                rescore(def, t1, t2, ts);
+                has_def = false;
+            }
+            __syncthreads();
+            if (tid == 0) s_pend_n = 0;
+            if (s_buf_n > 0) {
+                cta_sort_desc(E, A.sort_n);
+                for (uint32_t i = A.kpad + tid; i < A.sort_n; i += kThreads) E[i] = Entry{0ull, 0ull};
+                if (tid == 0) {
+                    s_buf_n = 0;
+                    const Entry kth = E[A.keep - 1];
+                    if (kth.k1 != 0ull) {
+                        s_t1 = kth.k1;
+                        s_t2 = kth.k2;
+                        const unsigned int ok = static_cast<unsigned int>(kth.k1 >> 32);
+                        s_ts = okey_score(ok);
+                        atomicMax(&A.ctrl->gtau, ok);
+                    }
                 }
             }
             __syncthreads();
         }
         if (!any) break;
-        if (has_def) {
-            const unsigned int slot = atomicAdd(&s_buf_n, 1u);
-            buf[slot] = def;
-            has_def = false;
-        }
-        unsigned long long t1 = s_t1, t2 = s_t2;
+        unsigned long long t1 = s_t1;
         float ts = s_ts;
         if ((round++ & 7u) == 0) gk = *reinterpret_cast<volatile unsigned int *>(&A.ctrl->gtau);
         if ((static_cast<unsigned long long>(gk) << 32) > t1) {
             t1 = static_cast<unsigned long long>(gk) << 32;
-            t2 = 0;
             ts = okey_score(gk);
         }
         const float tlo = __fsub_rd(ts, fmaxf(__fmul_ru(P.band, fabsf(ts)), P.err_abs));
@@ -1148,21 +1185,12 @@ __global__ void __launch_bounds__(kThreads, 3) screen_tc_kernel(const __grid_con
 #pragma unroll
                 for (int i = 0; i < 16; ++i) s = __fmaf_rn(x[i], y[i], s);
                 if (s >= tlo) {
-                    const float sf = static_cast<float>(score64_at<kFastDelta>(&A.m, &A.sc, el, seed_t, p));
-                    ++exact;
-                    if (sf >= ts) {
-                        const unsigned long long k1 = (static_cast<unsigned long long>(score_okey(sf)) << 32) |
-                                                      static_cast<unsigned int>(~item);
-                        const unsigned long long k2 = (static_cast<unsigned long long>(~dcand) << 32) | ddraw;
-                        if (k1 > t1 || (k1 == t1 && k2 > t2)) {
-                            const unsigned int slot = atomicAdd(&s_buf_n, 1u);
-                            if (slot < A.buf_cap) {
-                                buf[slot] = Entry{k1, k2};
-                            } else {
-                                has_def = true;
-                                def = Entry{k1, k2};
-                            }
-                        }
+                    const unsigned int slot = atomicAdd(&s_pend_n, 1u);
+                    if (slot < kPendCap) {
+                        pend[slot] = Pend{item, dcand, ddraw};
+                    } else {
+                        has_def = true;
+                        def = Pend{item, dcand, ddraw};
                     }
                 }
                 p += len;
