@@ -223,7 +223,9 @@ def run_islands(args):
     elites = [d["elites"] for d in isl]
     total = sum(c.lambda_ for c in cfgs)
     t0 = time.perf_counter()
-    best, table = autotune.autotune(cfgs, models, elites, scale=0.1, reps=2)
+    # tuned on the batch itself (full budgets) over the plausible settings
+    cands = [islands.Tune(), islands.Tune(ctas_per_sm=2), islands.Tune(seg_cands=131072)]
+    best, table = autotune.autotune(cfgs, models, elites, candidates=cands, scale=1.0, reps=1)
     tune_s = time.perf_counter() - t0
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     for _ in range(max(3, args.warmup)):

@@ -47,6 +47,35 @@ struct SynthConst {
 
 __host__ __device__ constexpr int tri(int i, int j) { return i * (i + 1) / 2 + j; }
 
+// The same coefficients in the order synth_score's filter form consumes them,
+// each gene's group starting on 16 bytes so that a shared-memory copy is read
+// with 16-byte loads: row k < 16 holds Wq[k][0..k] then w_lin[k]; then
+// w_lin[16..28]; then w16 and w0.
+__host__ __device__ constexpr int row_off(int k) {
+    int o = 0;
+    for (int j = 0; j < k; ++j) o += ((j + 2 + 3) / 4) * 4;
+    return o;
+}
+constexpr int kRowLin16 = row_off(16);      // 176
+constexpr int kRowW16 = kRowLin16 + 16;     // 192
+constexpr int kRowModelFloats = kRowW16 + 4;
+
+struct alignas(16) RowModel {
+    float v[kRowModelFloats];
+};
+
+// Coefficient access for synth_score: kernel-parameter DevModel or RowModel.
+__device__ __forceinline__ float m_q(const DevModel &M, int k, int l) { return M.wq[tri(k, l)]; }
+__device__ __forceinline__ float m_lin(const DevModel &M, int k) { return M.wlin[k]; }
+__device__ __forceinline__ float m_w0(const DevModel &M) { return M.w0; }
+__device__ __forceinline__ float m_w16(const DevModel &M) { return M.w16; }
+__device__ __forceinline__ float m_q(const RowModel &M, int k, int l) { return M.v[row_off(k) + l]; }
+__device__ __forceinline__ float m_lin(const RowModel &M, int k) {
+    return k < 16 ? M.v[row_off(k) + k + 1] : M.v[kRowLin16 + k - 16];
+}
+__device__ __forceinline__ float m_w0(const RowModel &M) { return M.v[kRowW16 + 1]; }
+__device__ __forceinline__ float m_w16(const RowModel &M) { return M.v[kRowW16]; }
+
 // y = z * kMix1 where z = s ^ (s >> 30): the first half of the mixer.
 __device__ __forceinline__ uint64_t mix_a(uint64_t s) {
     const uint64_t z = s ^ (s >> 30);
@@ -130,8 +159,8 @@ __device__ __forceinline__ CandHead cand_head(const SynthConst &C, uint64_t seed
 // sum_{k>=16} w_k g_k (165 FFMA). Both orders are within gamma_n * A of the
 // real value (A = sum of |terms|), so the host bounds |fast - exact| and the
 // exact order is evaluated only for candidates the bound cannot rule out.
-template <bool kFastDelta, bool kKeepGenes, bool kExact = true>
-__device__ __forceinline__ float synth_score(const DevModel &M, const SynthConst &C,
+template <bool kFastDelta, bool kKeepGenes, bool kExact = true, class Model = DevModel>
+__device__ __forceinline__ float synth_score(const Model &M, const SynthConst &C,
                                              const float *__restrict__ el, uint64_t seed_t,
                                              uint64_t p, const CandHead &h, float *genes) {
     const uint64_t s0 = seed_t + (p + 1) * kGolden;
@@ -146,7 +175,7 @@ __device__ __forceinline__ float synth_score(const DevModel &M, const SynthConst
     uint64_t su = s0 + (h.imm ? 3ull : 4ull) * kGolden;  // unit draw of gene 0
 
     float G[16], S[16];
-    float R = kExact ? 0.0f : M.w16;
+    float R = kExact ? 0.0f : m_w16(M);
 #pragma unroll
     for (int k = 0; k < kNtot; ++k) {
         const uint32_t bw = draw_bitword(su - kGolden);  // crossover bit draw
@@ -174,19 +203,19 @@ __device__ __forceinline__ float synth_score(const DevModel &M, const SynthConst
             if (k < 16) {
                 G[k] = g;
 #pragma unroll
-                for (int l = 0; l < k; ++l) S[l] = __fmaf_rn(M.wq[tri(k, l)], g, S[l]);
-                S[k] = __fmaf_rn(M.wq[tri(k, k)], g, M.wlin[k]);
+                for (int l = 0; l < k; ++l) S[l] = __fmaf_rn(m_q(M, k, l), g, S[l]);
+                S[k] = __fmaf_rn(m_q(M, k, k), g, m_lin(M, k));
             } else {
-                R = __fmaf_rn(M.wlin[k], g, R);
+                R = __fmaf_rn(m_lin(M, k), g, R);
             }
         } else if (k < 16) {
             G[k] = g;
 #pragma unroll
             for (int l = 0; l < k; ++l)
-                S[l] = __fadd_rn(S[l], __fmul_rn(M.wq[tri(k, l)], __fmul_rn(G[l], g)));
-            S[k] = __fadd_rn(0.0f, __fmul_rn(M.wq[tri(k, k)], __fmul_rn(g, g)));
+                S[l] = __fadd_rn(S[l], __fmul_rn(m_q(M, k, l), __fmul_rn(G[l], g)));
+            S[k] = __fadd_rn(0.0f, __fmul_rn(m_q(M, k, k), __fmul_rn(g, g)));
         } else {
-            const float t = __fmul_rn(M.wlin[k], g);
+            const float t = __fmul_rn(m_lin(M, k), g);
             R = (k == 16) ? __fadd_rn(0.0f, t) : __fadd_rn(R, t);
         }
     }
@@ -195,10 +224,10 @@ __device__ __forceinline__ float synth_score(const DevModel &M, const SynthConst
         for (int l = 0; l < 16; ++l) R = __fmaf_rn(G[l], S[l], R);
         return R;
     }
-    float r = __fadd_rn(__fadd_rn(M.w0, __fmul_rn(M.wlin[0], G[0])), S[0]);
+    float r = __fadd_rn(__fadd_rn(m_w0(M), __fmul_rn(m_lin(M, 0), G[0])), S[0]);
 #pragma unroll
     for (int l = 1; l < 16; ++l)
-        r = __fadd_rn(r, __fadd_rn(__fadd_rn(M.w0, __fmul_rn(M.wlin[l], G[l])), S[l]));
+        r = __fadd_rn(r, __fadd_rn(__fadd_rn(m_w0(M), __fmul_rn(m_lin(M, l), G[l])), S[l]));
     return __fadd_rn(r, R);
 }
 

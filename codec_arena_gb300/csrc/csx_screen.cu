@@ -1906,6 +1906,7 @@ constexpr int kMaxIslands = CSX_MAX_ISLANDS;
 
 struct IslandDev {
     DevModel m;
+    RowModel rm;  // the same coefficients in the screen's consumption order
     SynthConst sc;
     uint64_t seed;
     const float *el;  // (ne + 1) x 29 elite table
@@ -1953,7 +1954,7 @@ __device__ __forceinline__ uint32_t island_of(const unsigned int *b, uint32_t n,
 }
 
 template <bool kFastDelta>
-__device__ __noinline__ float exact_score_isl(const DevModel *m, const SynthConst *sc, const float *el,
+__device__ __noinline__ float exact_score_isl(const RowModel *m, const SynthConst *sc, const float *el,
                                               uint64_t seed_t, uint64_t p) {
     const CandHead h = cand_head(*sc, seed_t, p);
     return synth_score<kFastDelta, false, true>(*m, *sc, el, seed_t, p, h, nullptr);
@@ -1964,7 +1965,7 @@ __global__ void __launch_bounds__(kThreads, 3) screen_batch_kernel(const __grid_
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Entry *E = reinterpret_cast<Entry *>(smem_raw);
     float *el = reinterpret_cast<float *>(E + B.sort_n);
-    __shared__ DevModel s_m;
+    __shared__ RowModel s_m;
     __shared__ SynthConst s_sc;
     __shared__ unsigned int s_base[kMaxIslands + 1];
     __shared__ const Item *s_items;
@@ -2042,9 +2043,9 @@ __global__ void __launch_bounds__(kThreads, 3) screen_batch_kernel(const __grid_
             const unsigned int nx = s_next;
             if (nx == 0xFFFFFFFFu) break;
             const IslandDev *I = B.isl + nx;
-            const uint32_t *src = reinterpret_cast<const uint32_t *>(&I->m);
+            const uint32_t *src = reinterpret_cast<const uint32_t *>(&I->rm);
             uint32_t *dst = reinterpret_cast<uint32_t *>(&s_m);
-            for (uint32_t i = tid; i < sizeof(DevModel) / 4; i += kThreads) dst[i] = src[i];
+            for (uint32_t i = tid; i < sizeof(RowModel) / 4; i += kThreads) dst[i] = src[i];
             const uint32_t ne = I->ne;
             for (uint32_t i = tid; i < (ne + 1) * kNtot; i += kThreads) el[i] = I->el[i];
             for (uint32_t i = tid; i < B.sort_n; i += kThreads) E[i] = Entry{0ull, 0ull};
@@ -2199,6 +2200,18 @@ SynthConst make_synth(const csx_cfg &cfg, int ne) {
     return sc;
 }
 
+RowModel make_row_model(const DevModel &m) {
+    RowModel r{};
+    for (int k = 0; k < 16; ++k) {
+        for (int l = 0; l <= k; ++l) r.v[row_off(k) + l] = m.wq[tri(k, l)];
+        r.v[row_off(k) + k + 1] = m.wlin[k];
+    }
+    for (int k = 16; k < kNtot; ++k) r.v[kRowLin16 + k - 16] = m.wlin[k];
+    r.v[kRowW16] = m.w16;
+    r.v[kRowW16 + 1] = m.w0;
+    return r;
+}
+
 DevModel make_dev_model(const csx_model &model) {
     DevModel m;
     m.w0 = model.w0;
@@ -2351,6 +2364,7 @@ int batch_prepare(Context &cx, int n, const csx_cfg *cfgs, const csx_model *mode
         g += n_elites[i];
         IslandDev &d = hd[i];
         d.m = make_dev_model(models[i]);
+        d.rm = make_row_model(d.m);
         d.sc = make_synth(cfgs[i], n_elites[i]);
         d.seed = cfgs[i].seed;
         d.el = b.tab;
