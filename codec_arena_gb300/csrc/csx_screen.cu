@@ -45,7 +45,7 @@
 namespace csx {
 
 constexpr int kThreads = 256;      // screen CTA
-constexpr int kRounds = 8;         // candidates per thread between CTA barriers
+constexpr int kRounds = 16;        // candidates per thread between CTA barriers
 constexpr uint32_t kMaxKeep = 4096;
 constexpr uint32_t kMaxElites = 1536;
 constexpr uint64_t kLinkCap = 1ull << 26;
