@@ -49,7 +49,7 @@ constexpr int kRounds = 16;        // candidates per thread between CTA barriers
 constexpr uint32_t kMaxKeep = 4096;
 constexpr uint32_t kMaxElites = 1536;
 constexpr uint64_t kLinkCap = 1ull << 26;
-constexpr uint32_t kDefaultSegCands = 32768;
+constexpr uint32_t kDefaultSegCands = 65536;
 
 enum : uint32_t { kErrLink = 1u, kErrAssemble = 2u, kErrRegen = 4u, kErrItems = 8u };
 enum : uint32_t { kSegOk = 0, kSegLast = 1, kSegFail = 2 };
@@ -1336,10 +1336,11 @@ int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int
         if (rc) return rc;
     }
 
-    // item size D: about eight items per screen thread
+    // item size D: about 32 items per screen thread (measured: smaller items
+    // shorten the tail of the persistent grid more than their reads cost)
     uint64_t d = item_cands ? item_cands : env_u64("CSX_ITEM_CANDS", 0);
     if (d == 0) {
-        const uint64_t target = 8ull * static_cast<uint64_t>(pl->grid) * kThreads;
+        const uint64_t target = 32ull * static_cast<uint64_t>(pl->grid) * kThreads;
         d = std::max<uint64_t>(1, cfg.lambda / target);
         d = std::min<uint64_t>(16384, std::max<uint64_t>(64, d));
     }

@@ -159,7 +159,7 @@ int csx_screen_device(const csx_cfg *cfg, const csx_model *model, const csx_geno
  * library, which every GPU that loads the library holds until the process
  * exits. Configurations needing more scratch return CSX_ERR_LIMIT with a
  * message naming the bytes needed (the 2.65e9-candidate, T = 4, keep 256
- * generation needs about 19 MiB). The first call on a device looks up the
+ * generation needs about 14 MiB). The first call on a device looks up the
  * array's device address; make that first call before any stream capture.
  * All calls share the array: calls that overlap on the GPU race, so order
  * them (one stream, or events). Results equal csx_screen_device's. */
