@@ -11,7 +11,8 @@ result then equals the file-based path exactly.
 
 The format helpers mirror evolve.py's own: `load_pop` (:71-101),
 `genome_line` (:104-106), `features` (:211-220), `load_weights` (:223-241),
-`save_weights` (:244-247).
+`save_weights` (:244-247); the search-counter bookkeeping mirrors
+`screens_count.txt` (:621-622) and its merge in tools/merge_results.py:62-124.
 """
 from __future__ import annotations
 
@@ -149,5 +150,55 @@ def next_population(elites: Sequence[Dict], promoted: Sequence[Dict], *, shard: 
     return nxt
 
 
+def write_screens_count(out_dir: str, n_screens: int) -> str:
+    """brain/evolve.py:621-622: a shard's search counter file."""
+    import os
+
+    path = os.path.join(out_dir, "screens_count.txt")
+    with open(path, "w") as f:
+        f.write(str(int(n_screens)))
+    return path
+
+
+_EVAL_MILESTONES = [("1e5", 100_000), ("1e6", 1_000_000), ("1e7", 10_000_000), ("1e8", 100_000_000),
+                    ("1e9", 1_000_000_000)]
+_SEARCH_MILESTONES = [("1e6", 1_000_000), ("1e9", 1_000_000_000), ("1e12", 1_000_000_000_000)]
+
+
+def update_lifetime_counters(in_dir: str, state: Dict) -> Dict:
+    """The counter part of tools/merge_results.py:62-124: sum every shard's
+    evals_count.txt and screens_count.txt (shard-* directories of `in_dir`)
+    into `state` (lifetime_evals, search_evals = evals + screens, runs,
+    milestones); returns the updated copy."""
+    import glob
+    import os
+
+    n_evals = n_screens = 0
+    for sd in sorted(glob.glob(os.path.join(in_dir, "shard-*"))):
+        for name in ("evals_count.txt", "screens_count.txt"):
+            p = os.path.join(sd, name)
+            if os.path.exists(p):
+                with open(p) as f:
+                    v = int(f.read().strip() or 0)
+                if name == "evals_count.txt":
+                    n_evals += v
+                else:
+                    n_screens += v
+    st = dict(state) if state else {"lifetime_evals": 0, "runs": 0, "milestones": {}}
+    st.setdefault("search_evals", st.get("lifetime_evals", 0))
+    st["lifetime_evals"] = st.get("lifetime_evals", 0) + n_evals
+    st["search_evals"] += n_evals + n_screens
+    st["runs"] = st.get("runs", 0) + 1
+    st["milestones"] = dict(st.get("milestones", {}))
+    st["search_milestones"] = dict(st.get("search_milestones", {}))
+    for m, key in _EVAL_MILESTONES:
+        if st["lifetime_evals"] >= key and m not in st["milestones"]:
+            st["milestones"][m] = f"run {st['runs']}"
+    for m, key in _SEARCH_MILESTONES:
+        if st["search_evals"] >= key and m not in st["search_milestones"]:
+            st["search_milestones"][m] = f"run {st['runs']}"
+    return st
+
+
 __all__ = ["load_pop", "genome_line", "features", "load_weights", "save_weights", "elites_array",
-           "screen_generation", "next_population"]
+           "screen_generation", "next_population", "write_screens_count", "update_lifetime_counters"]

@@ -167,3 +167,24 @@ def test_in_process_direct_arrays(csx):
     assert screened == n == 300_000
     assert [p["pa"] for p in got] == want["pa"].tolist()
     np.testing.assert_array_equal(np.asarray([p["g"] for p in got], dtype=np.float32), want["g"])
+
+
+def test_search_counter_bookkeeping(tmp_path):
+    """screens_count.txt per shard, summed into the lifetime counters as
+    tools/merge_results.py does (search_evals = evals + screens)."""
+    from codec_arena_gb300 import brain
+
+    for i, (ev, sc) in enumerate([(120, 2_650_000_000 * 20), (80, 10**9), (0, None)]):
+        d = tmp_path / f"shard-{i}"
+        d.mkdir()
+        (d / "evals_count.txt").write_text(str(ev))
+        if sc is not None:
+            brain.write_screens_count(str(d), sc)
+    assert (tmp_path / "shard-0" / "screens_count.txt").read_text() == str(53_000_000_000)
+    st = brain.update_lifetime_counters(str(tmp_path), {"lifetime_evals": 99_950, "runs": 4, "milestones": {}})
+    assert st["lifetime_evals"] == 100_150 and st["runs"] == 5
+    assert st["search_evals"] == 99_950 + 200 + 54_000_000_000
+    assert st["milestones"] == {"1e5": "run 5"}
+    assert st["search_milestones"] == {"1e6": "run 5", "1e9": "run 5"}
+    st2 = brain.update_lifetime_counters(str(tmp_path), st)
+    assert st2["milestones"] == {"1e5": "run 5"} and st2["runs"] == 6
