@@ -71,6 +71,8 @@ def parse():
     ap.add_argument("--workload", default="generation", choices=["generation", "islands", "precision", "refit"],
                     help="islands: 20 islands batched in one graph launch (not the headline line)")
     ap.add_argument("--islands", type=int, default=20)
+    ap.add_argument("--islands-scale", type=float, default=1.0,
+                    help="scale every island budget (small cases for profiling)")
     return ap.parse_args()
 
 
@@ -218,7 +220,8 @@ def run_islands(args):
 
     torch.cuda.set_device(0)
     isl = wl.seeded_islands(args.islands)
-    cfgs = [screen.Cfg(d["lambda"], d["keep"], d["seed"], threads=d["threads"]) for d in isl]
+    cfgs = [screen.Cfg(max(1, int(d["lambda"] * args.islands_scale)), d["keep"], d["seed"], threads=d["threads"])
+            for d in isl]
     models = [screen.Model.from_compact(d["weights"]) for d in isl]
     elites = [d["elites"] for d in isl]
     total = sum(c.lambda_ for c in cfgs)
