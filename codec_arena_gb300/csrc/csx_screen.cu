@@ -94,8 +94,11 @@ struct Ctrl {
     unsigned long long exact_evals;  // reference-order evaluations (filter mode)
 };
 
+// Streams of one screen: T in all (src/screen.zig:267), of which this call
+// walks and screens the contiguous range [t0, t0 + nT) (all of them unless a
+// caller shards a generation by stream). Segment s is local to the range.
 struct StreamGeom {
-    uint64_t seed, T, per, my_last, L, n_seg;
+    uint64_t seed, T, per, my_last, L, n_seg, t0, nT;
     uint32_t C, C_last, d_log2, ckcap;
 };
 
@@ -103,10 +106,12 @@ __device__ __forceinline__ bool better(const Entry &a, const Entry &b) {
     return a.k1 > b.k1 || (a.k1 == b.k1 && a.k2 > b.k2);
 }
 
+// Segment s of the range -> global stream t and segment c within it.
 __device__ __forceinline__ void seg_of(const StreamGeom &g, uint64_t s, uint64_t &t, uint32_t &c) {
     t = s / g.C;
-    if (t > g.T - 1) t = g.T - 1;
+    if (t > g.nT - 1) t = g.nT - 1;
     c = static_cast<uint32_t>(s - t * g.C);
+    t += g.t0;
 }
 
 __device__ __forceinline__ uint64_t stream_seed(uint64_t seed, uint64_t t) {
@@ -304,12 +309,13 @@ __global__ void link_kernel(SynthConst sc, StreamGeom g, SegRec *__restrict__ re
 
 __global__ void assemble_kernel(StreamGeom g, const SegRec *__restrict__ recs, SegOut *__restrict__ outs,
                                 Ctrl *__restrict__ ctrl) {
-    const uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (t >= g.T) return;
+    const uint64_t tl = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (tl >= g.nT) return;
+    const uint64_t t = g.t0 + tl;
     const bool last_stream = t == g.T - 1;
     const uint64_t my = last_stream ? g.my_last : g.per;
     const uint32_t ct = last_stream ? g.C_last : g.C;
-    const uint64_t s0 = t * g.C;
+    const uint64_t s0 = tl * g.C;
     uint64_t lo = 0, pos = 0, idx = 0;
     bool bad = false;
     for (uint32_t c = 0; c < ct; ++c) {
@@ -363,11 +369,11 @@ __global__ void __launch_bounds__(kAsmThreads) assemble_block_kernel(StreamGeom 
     __shared__ unsigned long long carry;
     __shared__ int pending, failed;
     __shared__ uint64_t pend_lo, pend_pos;
-    const uint64_t t = blockIdx.x;
+    const uint64_t tl = blockIdx.x, t = g.t0 + tl;
     const bool last_stream = t == g.T - 1;
     const uint64_t my = last_stream ? g.my_last : g.per;
     const uint32_t ct = last_stream ? g.C_last : g.C;
-    const uint64_t s0 = t * g.C;
+    const uint64_t s0 = tl * g.C;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     if (tid == 0) {
         carry = 0;
@@ -569,15 +575,16 @@ __global__ void emit_kernel(StreamGeom g, const SegOut *__restrict__ outs, const
 
 // Streams no longer than one item: one item per stream, starting at draw 0.
 __global__ void stream_items_kernel(StreamGeom g, Item *__restrict__ items, Ctrl *__restrict__ ctrl) {
-    const uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (t == 0) ctrl->n_items = static_cast<unsigned int>(g.T);
-    if (t >= g.T) return;
+    const uint64_t tl = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (tl == 0) ctrl->n_items = static_cast<unsigned int>(g.nT);
+    if (tl >= g.nT) return;
+    const uint64_t t = g.t0 + tl;
     Item it;
     it.draw0 = 0;
     it.idx0 = 0;
     it.stream = static_cast<uint32_t>(t);
     it.n = static_cast<uint32_t>(t == g.T - 1 ? g.my_last : g.per);
-    items[t] = it;
+    items[tl] = it;
 }
 
 // ---- 4. screen ----------------------------------------------------------------
@@ -1298,7 +1305,8 @@ float filter_bound(const csx_model &m) {
 // grid_override, item_cands, seg_cands: 0 = automatic (the batched screen
 // passes its own grid and the tuner's sizes).
 int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int ne, Plan *pl,
-              int grid_override = 0, uint64_t item_cands = 0, uint64_t seg_cands = 0) {
+              int grid_override = 0, uint64_t item_cands = 0, uint64_t seg_cands = 0, uint64_t t_begin = 0,
+              uint64_t t_end = 0) {
     StreamGeom &g = pl->g;
     g.seed = cfg.seed;
     g.T = std::max<uint64_t>(1, std::min<uint64_t>(cfg.threads, cfg.lambda));  // src/screen.zig:267
@@ -1306,6 +1314,12 @@ int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int
     g.my_last = cfg.lambda - (g.T - 1) * g.per;
     const uint64_t my_max = std::max(g.per, g.my_last);
     if (g.T >= 0xFFFFFFFFull) return CSX_ERR_LIMIT;
+    if (t_end == 0) t_end = g.T;  // the whole generation
+    if (t_begin >= t_end || t_end > g.T) return CSX_ERR_BAD_ARGS;
+    g.t0 = t_begin;
+    g.nT = t_end - t_begin;
+    const bool has_last = t_end == g.T;
+    const uint64_t lam_range = (g.nT - (has_last ? 1 : 0)) * g.per + (has_last ? g.my_last : 0);
     pl->fast_delta = std::isfinite(cfg.sigma) && std::fabs(cfg.sigma) <= 1.0e38f &&
                      (cfg.sigma == 0.0f || std::fabs(cfg.sigma) >= 1.0e-30f);
     pl->err = filter_bound(model);
@@ -1341,7 +1355,7 @@ int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int
     uint64_t d = item_cands ? item_cands : env_u64("CSX_ITEM_CANDS", 0);
     if (d == 0) {
         const uint64_t target = 32ull * static_cast<uint64_t>(pl->grid) * kThreads;
-        d = std::max<uint64_t>(1, cfg.lambda / target);
+        d = std::max<uint64_t>(1, lam_range / target);
         d = std::min<uint64_t>(16384, std::max<uint64_t>(64, d));
     }
     uint32_t dl = 0;
@@ -1360,10 +1374,10 @@ int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int
     g.L = L;
     g.C = static_cast<uint32_t>(std::max<uint64_t>(1, (64 * g.per + L - 1) / L));
     g.C_last = static_cast<uint32_t>(std::max<uint64_t>(1, (64 * g.my_last + L - 1) / L));
-    g.n_seg = (g.T - 1) * g.C + g.C_last;
+    g.n_seg = (g.nT - 1) * g.C + (has_last ? g.C_last : g.C);
     g.ckcap = static_cast<uint32_t>((2 * L / 33) / D + 3);
     pl->short_path = my_max <= D;
-    pl->items_cap = pl->short_path ? g.T : g.n_seg * (static_cast<uint64_t>(g.ckcap) + 1);
+    pl->items_cap = pl->short_path ? g.nT : g.n_seg * (static_cast<uint64_t>(g.ckcap) + 1);
     if (pl->items_cap >= 0xFFFFFFFFull) return CSX_ERR_LIMIT;
     return CSX_OK;
 }
@@ -1372,9 +1386,10 @@ int unit_blocks(uint64_t n, int threads) { return static_cast<int>((n + threads 
 
 // Enqueue the whole pipeline on `st`. Device inputs: genomes (csx_genome x ne).
 int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, const csx_genome *d_genomes,
-                   int ne, csx_survivor *d_out, unsigned long long *d_result, cudaStream_t st) {
+                   int ne, csx_survivor *d_out, unsigned long long *d_result, cudaStream_t st,
+                   uint64_t t_begin = 0, uint64_t t_end = 0) {
     Plan pl;
-    int rc = make_plan(cx, cfg, model, ne, &pl);
+    int rc = make_plan(cx, cfg, model, ne, &pl, 0, 0, 0, t_begin, t_end);
     if (rc) return rc;
     const StreamGeom &g = pl.g;
     const bool fast = pl.fast_delta;
@@ -1426,7 +1441,7 @@ int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, cons
 
     Item *items = static_cast<Item *>(cx.items.p);
     if (pl.short_path) {
-        stream_items_kernel<<<unit_blocks(g.T, 256), 256, 0, st>>>(g, items, ctrl);
+        stream_items_kernel<<<unit_blocks(g.nT, 256), 256, 0, st>>>(g, items, ctrl);
         CSX_CUDA(cudaGetLastError());
         ++launches;
     } else {
@@ -1439,9 +1454,9 @@ int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, cons
         link_kernel<<<unit_blocks(g.n_seg * 32, 128), 128, 0, st>>>(sc, g, recs, ck, ctrl);
         CSX_CUDA(cudaGetLastError());
         if (g.C >= 64)
-            assemble_block_kernel<<<static_cast<unsigned>(g.T), kAsmThreads, 0, st>>>(g, recs, so, ctrl);
+            assemble_block_kernel<<<static_cast<unsigned>(g.nT), kAsmThreads, 0, st>>>(g, recs, so, ctrl);
         else
-            assemble_kernel<<<unit_blocks(g.T, 128), 128, 0, st>>>(g, recs, so, ctrl);
+            assemble_kernel<<<unit_blocks(g.nT, 128), 128, 0, st>>>(g, recs, so, ctrl);
         CSX_CUDA(cudaGetLastError());
         scan_kernel<<<1, 1024, 0, st>>>(so, g.n_seg, off, ctrl, pl.items_cap);
         CSX_CUDA(cudaGetLastError());
@@ -1595,8 +1610,14 @@ int csx_screen_device(const csx_cfg *cfg, const csx_model *model, const csx_geno
                           reinterpret_cast<unsigned long long *>(d_result), st);
 }
 
-int csx_screen(const csx_cfg *cfg, const csx_model *model, const csx_genome *elites, int n_elites,
-               csx_survivor *out, uint64_t out_cap, uint64_t *n_out, uint64_t *screened) {
+}  // extern "C"
+
+namespace csx {
+
+// csx_screen / csx_screen_range: host buffers, a private stream, synchronous.
+int screen_host(const csx_cfg *cfg, const csx_model *model, const csx_genome *elites, int n_elites,
+                uint64_t t_begin, uint64_t t_end, csx_survivor *out, uint64_t out_cap, uint64_t *n_out,
+                uint64_t *screened) {
     if (n_out) *n_out = 0;
     if (screened) *screened = 0;
     int rc = check_common(cfg, model, n_elites);
@@ -1625,7 +1646,7 @@ int csx_screen(const csx_cfg *cfg, const csx_model *model, const csx_genome *eli
     cudaError_t e = cudaMemcpyAsync(dg, elites, static_cast<size_t>(n_elites) * sizeof(csx_genome),
                                     cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) {
-        rc = enqueue_screen(*cx, *cfg, *model, dg, n_elites, ds, dr, st);
+        rc = enqueue_screen(*cx, *cfg, *model, dg, n_elites, ds, dr, st, t_begin, t_end);
         if (rc == CSX_OK) {
             e = cudaMemcpyAsync(res, dr, sizeof(res), cudaMemcpyDeviceToHost, st);
             if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -1650,6 +1671,26 @@ int csx_screen(const csx_cfg *cfg, const csx_model *model, const csx_genome *eli
     *n_out = (cfg->flags & CSX_FLAG_AS_SHIPPED) ? 0 : std::min<uint64_t>(res[0], keep_n);
     if (screened) *screened = res[1];
     return CSX_OK;
+}
+
+}  // namespace csx
+
+extern "C" {
+
+int csx_screen(const csx_cfg *cfg, const csx_model *model, const csx_genome *elites, int n_elites,
+               csx_survivor *out, uint64_t out_cap, uint64_t *n_out, uint64_t *screened) {
+    return screen_host(cfg, model, elites, n_elites, 0, 0, out, out_cap, n_out, screened);
+}
+
+int csx_screen_range(const csx_cfg *cfg, const csx_model *model, const csx_genome *elites, int n_elites,
+                     uint64_t t_begin, uint64_t t_end, csx_survivor *out, uint64_t out_cap, uint64_t *n_out,
+                     uint64_t *screened) {
+    if (t_end <= t_begin) {
+        if (n_out) *n_out = 0;
+        if (screened) *screened = 0;
+        return CSX_ERR_BAD_ARGS;
+    }
+    return screen_host(cfg, model, elites, n_elites, t_begin, t_end, out, out_cap, n_out, screened);
 }
 
 }  // extern "C"
@@ -1704,6 +1745,8 @@ int plan_noalloc(const NoAllocDevice &dv, const csx_cfg &cfg, const csx_model &m
     g.T = std::max<uint64_t>(1, std::min<uint64_t>(cfg.threads, cfg.lambda));
     g.per = cfg.lambda / g.T;
     g.my_last = cfg.lambda - (g.T - 1) * g.per;
+    g.t0 = 0;
+    g.nT = g.T;
     const uint64_t my_max = std::max(g.per, g.my_last);
     if (g.T >= 0xFFFFFFFFull) return CSX_ERR_LIMIT;
     pl->fast_delta = std::isfinite(cfg.sigma) && std::fabs(cfg.sigma) <= 1.0e38f &&
@@ -1737,7 +1780,7 @@ int plan_noalloc(const NoAllocDevice &dv, const csx_cfg &cfg, const csx_model &m
     g.n_seg = (g.T - 1) * g.C + g.C_last;
     g.ckcap = static_cast<uint32_t>((L / 33) / D + 3);
     pl->short_path = my_max <= D;
-    pl->items_cap = pl->short_path ? g.T : 2 * g.n_seg + cfg.lambda / D + 1;
+    pl->items_cap = pl->short_path ? g.nT : 2 * g.n_seg + cfg.lambda / D + 1;
     if (pl->items_cap >= 0xFFFFFFFFull) return CSX_ERR_LIMIT;
     return CSX_OK;
 }
@@ -1802,7 +1845,7 @@ int enqueue_screen_noalloc(const NoAllocDevice &dv, const csx_cfg &cfg, const cs
         d_genomes, ne, tab, ids, tribes);
     CSX_CUDA(cudaGetLastError());
     if (pl.short_path) {
-        stream_items_kernel<<<unit_blocks(g.T, 256), 256, 0, st>>>(g, items, ctrl);
+        stream_items_kernel<<<unit_blocks(g.nT, 256), 256, 0, st>>>(g, items, ctrl);
         CSX_CUDA(cudaGetLastError());
     } else {
         walk_kernel<<<unit_blocks(g.n_seg, 128), 128, 0, st>>>(sc, g, recs, ck, ctrl);
@@ -1810,9 +1853,9 @@ int enqueue_screen_noalloc(const NoAllocDevice &dv, const csx_cfg &cfg, const cs
         link_kernel<<<unit_blocks(g.n_seg * 32, 128), 128, 0, st>>>(sc, g, recs, ck, ctrl);
         CSX_CUDA(cudaGetLastError());
         if (g.C >= 64)
-            assemble_block_kernel<<<static_cast<unsigned>(g.T), kAsmThreads, 0, st>>>(g, recs, so, ctrl);
+            assemble_block_kernel<<<static_cast<unsigned>(g.nT), kAsmThreads, 0, st>>>(g, recs, so, ctrl);
         else
-            assemble_kernel<<<unit_blocks(g.T, 128), 128, 0, st>>>(g, recs, so, ctrl);
+            assemble_kernel<<<unit_blocks(g.nT, 128), 128, 0, st>>>(g, recs, so, ctrl);
         CSX_CUDA(cudaGetLastError());
         scan_kernel<<<1, 1024, 0, st>>>(so, g.n_seg, off, ctrl, pl.items_cap);
         CSX_CUDA(cudaGetLastError());
@@ -2413,7 +2456,7 @@ int batch_enqueue(Context &cx, const BatchLayout &L, cudaStream_t st, bool captu
         if (L.cfg[i].lambda > 0) {
             const SynthConst sc = make_synth(L.cfg[i], ne);
             if (pl.short_path) {
-                stream_items_kernel<<<unit_blocks(g.T, 256), 256, 0, a>>>(g, b.items, b.ctrl);
+                stream_items_kernel<<<unit_blocks(g.nT, 256), 256, 0, a>>>(g, b.items, b.ctrl);
                 CSX_CUDA(cudaGetLastError());
                 ++nk;
             } else {
@@ -2422,9 +2465,9 @@ int batch_enqueue(Context &cx, const BatchLayout &L, cudaStream_t st, bool captu
                 link_kernel<<<unit_blocks(g.n_seg * 32, 128), 128, 0, a>>>(sc, g, b.recs, b.ck, b.ctrl);
                 CSX_CUDA(cudaGetLastError());
                 if (g.C >= 64)
-                    assemble_block_kernel<<<static_cast<unsigned>(g.T), kAsmThreads, 0, a>>>(g, b.recs, b.so, b.ctrl);
+                    assemble_block_kernel<<<static_cast<unsigned>(g.nT), kAsmThreads, 0, a>>>(g, b.recs, b.so, b.ctrl);
                 else
-                    assemble_kernel<<<unit_blocks(g.T, 128), 128, 0, a>>>(g, b.recs, b.so, b.ctrl);
+                    assemble_kernel<<<unit_blocks(g.nT, 128), 128, 0, a>>>(g, b.recs, b.so, b.ctrl);
                 CSX_CUDA(cudaGetLastError());
                 scan_kernel<<<1, 1024, 0, a>>>(b.so, g.n_seg, b.off, b.ctrl, pl.items_cap);
                 CSX_CUDA(cudaGetLastError());

@@ -96,17 +96,26 @@ def _elites_array(elites) -> np.ndarray:
     return e
 
 
-def screen(cfg: Cfg, model: Model, elites) -> Tuple[np.ndarray, int]:
-    """run() without the file output: (survivors sorted by score desc, screened)."""
+def screen(cfg: Cfg, model: Model, elites, streams: Optional[Tuple[int, int]] = None) -> Tuple[np.ndarray, int]:
+    """run() without the file output: (survivors sorted by score desc, screened).
+
+    streams=(a, b) screens only RNG streams a..b-1 of the generation (one
+    rank's share when a generation is sharded by stream; merge the ranks'
+    survivors with parallel.merge_survivors)."""
     e = _elites_array(elites)
     keep_n = min(int(cfg.keep), int(cfg.lambda_))
     out = np.zeros(max(keep_n, 1), dtype=SURVIVOR_DTYPE)
     n_out = ctypes.c_uint64(0)
     screened = ctypes.c_uint64(0)
     c = cfg.c()
-    check(lib().csx_screen(ctypes.byref(c), ctypes.byref(model.c), e.ctypes.data, int(e.shape[0]),
-                           out.ctypes.data, keep_n, ctypes.byref(n_out), ctypes.byref(screened)),
-          "screen")
+    if streams is None:
+        check(lib().csx_screen(ctypes.byref(c), ctypes.byref(model.c), e.ctypes.data, int(e.shape[0]),
+                               out.ctypes.data, keep_n, ctypes.byref(n_out), ctypes.byref(screened)),
+              "screen")
+    else:
+        check(lib().csx_screen_range(ctypes.byref(c), ctypes.byref(model.c), e.ctypes.data, int(e.shape[0]),
+                                     int(streams[0]), int(streams[1]), out.ctypes.data, keep_n,
+                                     ctypes.byref(n_out), ctypes.byref(screened)), "screen_range")
     return out[: n_out.value], int(screened.value)
 
 

@@ -142,6 +142,17 @@ int csx_screen(const csx_cfg *cfg, const csx_model *model, const csx_genome *eli
                int n_elites, csx_survivor *out, uint64_t out_cap, uint64_t *n_out,
                uint64_t *screened);
 
+/* csx_screen restricted to the RNG streams [t_begin, t_end) of the same
+ * generation (0 <= t_begin < t_end <= T, T = max(1, min(threads, lambda))):
+ * one rank's share when a generation is sharded by stream across GPUs.
+ * Survivors carry their global stream ids; the top-K of all ranks' survivors
+ * in the order score descending, (stream, index) ascending equals csx_screen's
+ * result. *screened counts the range's candidates. No reference counterpart
+ * (the reference runs every stream in one process). */
+int csx_screen_range(const csx_cfg *cfg, const csx_model *model, const csx_genome *elites, int n_elites,
+                     uint64_t t_begin, uint64_t t_end, csx_survivor *out, uint64_t out_cap, uint64_t *n_out,
+                     uint64_t *screened);
+
 /* Same, with device-resident elites and survivors, enqueued on `cuda_stream`
  * (a cudaStream_t; NULL = the legacy default stream). d_result receives four
  * device uint64: survivor count, screened count, device error bits (0 = ok)

@@ -1,7 +1,8 @@
 """Worker for tests/test_parallel.py, launched by torch.distributed.run with
-the gloo backend on CPU. Each rank screens its share of one generation's RNG
-streams with the CPU oracle (the checker stands in for the GPU engine here),
-then the ranks merge survivors and agree on the slowest rank's time."""
+the gloo backend. Each rank screens its share of one generation's RNG streams
+-- with the GPU engine (csx_screen_range) when the sixth argument is "gpu",
+else with the CPU oracle -- then the ranks merge survivors over gloo and agree
+on the slowest rank's time."""
 import json
 import os
 import sys
@@ -23,19 +24,27 @@ def main():
     rank, world = dist.get_rank(), dist.get_world_size()
     lam, keep, seed, T = int(sys.argv[1]), int(sys.argv[2]), int(sys.argv[3]), int(sys.argv[4])
     out = sys.argv[5]
+    engine = sys.argv[6] if len(sys.argv) > 6 else "oracle"
     el = wl.seeded_elites(16, seed=3)
-    m = oracle.model_from_compact(wl.surrogate_161())
-    c = oracle.cfg(lam, keep, seed, threads=T)
-    Tn = max(1, min(T, lam))
-    per = lam // Tn
     t0 = time.perf_counter()
-    local = []
-    for t in parallel.stream_ranges(T, lam, world)[rank]:
-        my = lam - (Tn - 1) * per if t == Tn - 1 else per
-        d = oracle.stream_dump(c, m, el, t, my)
-        d["index"] = np.arange(my)
-        local.append(d)
-    mine = parallel.merge_survivors(local, keep)
+    rg = parallel.stream_ranges(T, lam, world)[rank]
+    if engine == "gpu":
+        from codec_arena_gb300 import screen
+
+        mine, _ = screen.screen(screen.Cfg(lam, keep, seed, threads=T), screen.Model.from_compact(wl.surrogate_161()),
+                                el, streams=(rg.start, rg.stop))
+    else:
+        m = oracle.model_from_compact(wl.surrogate_161())
+        c = oracle.cfg(lam, keep, seed, threads=T)
+        Tn = max(1, min(T, lam))
+        per = lam // Tn
+        local = []
+        for t in rg:
+            my = lam - (Tn - 1) * per if t == Tn - 1 else per
+            d = oracle.stream_dump(c, m, el, t, my)
+            d["index"] = np.arange(my)
+            local.append(d)
+        mine = parallel.merge_survivors(local, keep)
     merged = parallel.gather_survivors(mine, keep)
     slowest = parallel.max_over_ranks(time.perf_counter() - t0 + rank)
     if rank == 0:

@@ -330,3 +330,35 @@ def test_late_meetings_block_assembly(orc, env):
     check(orc, 20_000_000, 128, 23, 4, wl.surrogate_161(), wl.seeded_elites(64))
     env.setenv("CSX_SEG_CANDS", "700")
     check(orc, 6_000_000, 64, 5, 3, wl.seeded_normal_model(), wl.seeded_elites(20), imm=0.05, jump=0.1)
+
+
+@pytest.mark.parametrize("lam,T,parts", [(30_000_000, 4, [(0, 1), (1, 2), (2, 3), (3, 4)]),
+                                         (30_000_000, 4, [(0, 3), (3, 4)]),
+                                         (5_000_003, 7, [(0, 2), (2, 7)]),
+                                         (90_000, 5, [(0, 4), (4, 5)]),
+                                         (1_000, 3, [(1, 3), (0, 1)])])
+def test_stream_ranges_merge_to_the_generation(lam, T, parts):
+    """csx_screen_range on a partition of the streams, merged in the
+    reference's order, equals the whole generation bit for bit."""
+    from codec_arena_gb300 import parallel, screen, workloads as wl
+
+    el = wl.seeded_elites(64)
+    m = screen.Model.from_compact(wl.surrogate_161())
+    cfg = screen.Cfg(lam, 128, 31, threads=T)
+    full, n = screen.screen(cfg, m, el)
+    pieces = [screen.screen(cfg, m, el, streams=p) for p in parts]
+    assert sum(p[1] for p in pieces) == n == lam
+    for (surv, _), (a, b) in zip(pieces, parts):
+        assert np.all((surv["stream"] >= a) & (surv["stream"] < b))
+    assert parallel.merge_survivors([p[0] for p in pieces], 128).tobytes() == full.tobytes()
+
+
+def test_stream_range_errors():
+    from codec_arena_gb300 import _lib, screen, workloads as wl
+
+    m = screen.Model.from_compact(wl.surrogate_161())
+    el = wl.seeded_elites(8)
+    for rg in [(2, 2), (3, 1), (0, 5)]:
+        with pytest.raises(_lib.CsxError) as e:
+            screen.screen(screen.Cfg(1000, 8, 1, threads=4), m, el, streams=rg)
+        assert e.value.status == _lib.ERR_BAD_ARGS

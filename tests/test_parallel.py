@@ -1,5 +1,7 @@
-"""Multi-rank host logic on CPU (gloo, world size 2): stream sharding of one
-generation and island seeding, checked against the single-process oracle."""
+"""Multi-rank logic (gloo, world size 2): stream sharding of one generation and
+island seeding, checked against the single-process oracle -- on CPU with the
+oracle screening each rank's streams, and (GPU-marked) with the GPU engine
+screening each rank's stream range."""
 import json
 import os
 import subprocess
@@ -45,6 +47,35 @@ def test_merge_equals_single_process(orc):
             local.append(d)
         parts.append(parallel.merge_survivors(local, keep))
     assert parallel.merge_survivors(parts, keep).tobytes() == full.tobytes()
+
+
+def _run_world_2(tmp_path, lam, keep, seed, T, engine, port):
+    out = tmp_path / f"rank0_{engine}.json"
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=2",
+           "--master-addr=127.0.0.1", f"--master-port={port}",
+           os.path.join(ROOT, "tests", "_dist_worker.py"), str(lam), str(keep), str(seed), str(T), str(out), engine]
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=300, env=env)
+    assert r.returncode == 0, r.stderr[-2000:]
+    return json.load(open(out))
+
+
+@pytest.mark.gpu
+def test_gloo_world_size_2_gpu_engine(orc, tmp_path):
+    """Two ranks, each screening its stream range on the GPU, merged over gloo:
+    equal to the oracle's single-process generation."""
+    from conftest import has_gpu
+
+    if not has_gpu():
+        pytest.skip("no CUDA device")
+    from codec_arena_gb300 import _lib, workloads as wl
+
+    lam, keep, seed, T = 3_000_001, 64, 8, 5
+    res = _run_world_2(tmp_path, lam, keep, seed, T, "gpu", 29534)
+    merged = np.frombuffer(bytes.fromhex(res["merged"]), dtype=_lib.SURVIVOR_DTYPE)
+    full, _ = orc.screen(orc.cfg(lam, keep, seed, threads=T), orc.model_from_compact(wl.surrogate_161()),
+                         wl.seeded_elites(16, seed=3))
+    assert merged.tobytes() == full.tobytes()
 
 
 def test_gloo_world_size_2(orc, tmp_path):
