@@ -51,7 +51,7 @@ THREADS = 4
 SEED = 7
 N_ELITES = 64
 # Algorithmic 32-bit lane-ops per candidate: 61.75 splitmix64 draws x 20 +
-# 29 genes x 5 + 181 FMA x 2 ("Roofline").
+# 29 genes x 5 + 181 FMA x 2: the candidate's RNG, gene arithmetic and scoring.
 LANE_OPS_PER_CAND = 1760.0
 DRAWS_PER_CAND = 61.75
 
