@@ -68,6 +68,13 @@ struct Entry {
     unsigned long long k1, k2;
 };
 
+// A candidate waiting for a second, more exact score (its item, its index in
+// the item, its draw offset): the queues of the filter and precision forms.
+struct Pend {
+    uint32_t item, dcand, ddraw;
+};
+constexpr uint32_t kPendCap = 512;  // queue entries per CTA
+
 struct SegRec {
     uint64_t merge_pos;  // first draw shared by this chain and the next segment's
     uint32_t n;          // chain candidates starting inside the segment
@@ -772,6 +779,162 @@ __global__ void __launch_bounds__(kThreads, 3) screen_kernel(const __grid_consta
     }
 }
 
+// The filter form with the reference-order evaluation deferred: a candidate
+// whose filter score is within the bound of the threshold goes to a shared
+// queue, and at the next merge all threads evaluate the queue in the
+// reference's f32 order -- whole warps, instead of one lane evaluating while
+// the other 31 of its warp wait. The buffer fills only from the queue, and
+// every fill is sorted at once, so it always has room (queue + one held entry
+// per thread <= 768 <= sort_n - kpad).
+template <bool kFastDelta>
+__global__ void __launch_bounds__(kThreads, 3) screen_q_kernel(const __grid_constant__ ScreenArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Entry *E = reinterpret_cast<Entry *>(smem_raw);
+    float *el = reinterpret_cast<float *>(E + A.sort_n);
+    Pend *pend = reinterpret_cast<Pend *>(el + (A.sc.ne + 1) * kNtot);
+    __shared__ unsigned int s_buf_n, s_pend_n;
+    __shared__ unsigned long long s_t1, s_t2;
+    __shared__ float s_ts;
+
+    const uint32_t tid = threadIdx.x;
+    for (uint32_t i = tid; i < A.sort_n; i += kThreads) E[i] = Entry{0ull, 0ull};
+    for (uint32_t i = tid; i < (A.sc.ne + 1) * kNtot; i += kThreads) el[i] = A.el[i];
+    if (tid == 0) {
+        s_buf_n = 0;
+        s_pend_n = 0;
+        s_t1 = 0;
+        s_t2 = 0;
+        s_ts = -INFINITY;
+    }
+    const unsigned int n_items = *reinterpret_cast<volatile unsigned int *>(&A.ctrl->n_items);
+    __syncthreads();
+
+    Entry *buf = E + A.kpad;
+    uint32_t item = atomicAdd(&A.ctrl->next_item, 1u);
+    bool valid = item < n_items;
+    uint64_t seed_t = 0, p = 0;
+    uint32_t left = 0, dcand = 0, ddraw = 0;
+    if (valid) {
+        const Item it = A.items[item];
+        seed_t = stream_seed(A.seed, it.stream);
+        p = it.draw0;
+        left = it.n;
+        valid = left > 0;
+    }
+    unsigned long long screened = 0, exact = 0;
+    unsigned int gk = 0;
+    uint32_t round = 0;
+    bool has_def = false;  // holds a candidate the full queue could not take; pauses until the merge
+    Pend def{0u, 0u, 0u};
+
+    auto rescore = [&](const Pend &q, unsigned long long t1, unsigned long long t2, float ts) {
+        const Item it = A.items[q.item];
+        const float s = exact_score_at<kFastDelta>(&A, el, stream_seed(A.seed, it.stream), it.draw0 + q.ddraw);
+        ++exact;
+        if (s >= ts) {
+            const unsigned long long k1 =
+                (static_cast<unsigned long long>(score_okey(s)) << 32) | static_cast<unsigned int>(~q.item);
+            const unsigned long long k2 = (static_cast<unsigned long long>(~q.dcand) << 32) | q.ddraw;
+            if (k1 > t1 || (k1 == t1 && k2 > t2)) buf[atomicAdd(&s_buf_n, 1u)] = Entry{k1, k2};
+        }
+    };
+
+    // merge the buffer into the CTA's sorted list; publishes the threshold
+    auto merge = [&]() {
+        cta_sort_desc(E, A.sort_n);
+        for (uint32_t i = A.kpad + tid; i < A.sort_n; i += kThreads) E[i] = Entry{0ull, 0ull};
+        if (tid == 0) {
+            s_buf_n = 0;
+            const Entry kth = E[A.keep - 1];
+            if (kth.k1 != 0ull) {
+                s_t1 = kth.k1;
+                s_t2 = kth.k2;
+                const unsigned int ok = static_cast<unsigned int>(kth.k1 >> 32);
+                s_ts = okey_score(ok);
+                atomicMax(&A.ctrl->gtau, ok);
+            }
+        }
+        __syncthreads();
+    };
+
+    for (;;) {
+        __syncthreads();
+        const unsigned int pn = min(s_pend_n, kPendCap);
+        const int any = __syncthreads_or(valid || has_def);
+        const int any_def = __syncthreads_or(has_def);
+        // the queue is evaluated once it can employ every thread (or a thread
+        // waits on it, or the work is done); a flush appends <= pn + 256 <= 768
+        if (pn >= kThreads || any_def || (!any && pn > 0)) {
+            if (s_buf_n + kPendCap + kThreads > A.buf_cap) merge();  // make room first
+            unsigned long long t1 = s_t1, t2 = s_t2;
+            float ts = s_ts;
+            const unsigned int g = *reinterpret_cast<volatile unsigned int *>(&A.ctrl->gtau);
+            if ((static_cast<unsigned long long>(g) << 32) > t1) {
+                t1 = static_cast<unsigned long long>(g) << 32;
+                t2 = 0;
+                ts = okey_score(g);
+            }
+            for (uint32_t i = tid; i < pn; i += kThreads) rescore(pend[i], t1, t2, ts);
+            if (has_def) {
+                rescore(def, t1, t2, ts);
+                has_def = false;
+            }
+            __syncthreads();
+            if (tid == 0) s_pend_n = 0;
+            __syncthreads();
+        }
+        const unsigned int bn = s_buf_n;
+        if (bn >= A.buf_cap / 2 || (!any && bn > 0)) merge();
+        if (!any) break;
+        float ts = s_ts;
+        const unsigned long long t1 = s_t1;
+        if ((round++ & 7u) == 0) gk = *reinterpret_cast<volatile unsigned int *>(&A.ctrl->gtau);
+        if ((static_cast<unsigned long long>(gk) << 32) > t1) ts = okey_score(gk);
+        const float tlo = __fsub_rd(ts, A.err);
+#pragma unroll 1
+        for (int r = 0; r < kRounds && valid && !has_def; ++r) {
+            const CandHead h = cand_head(A.sc, seed_t, p);
+            const float s = synth_score<kFastDelta, false, false>(A.m, A.sc, el, seed_t, p, h, nullptr);
+            if (s >= tlo) {
+                const unsigned int slot = atomicAdd(&s_pend_n, 1u);
+                if (slot < kPendCap) {
+                    pend[slot] = Pend{item, dcand, ddraw};
+                } else {
+                    has_def = true;
+                    def = Pend{item, dcand, ddraw};
+                }
+            }
+            p += h.len;
+            ddraw += h.len;
+            ++dcand;
+            ++screened;
+            if (--left == 0) {
+                item = atomicAdd(&A.ctrl->next_item, 1u);
+                valid = item < n_items;
+                if (valid) {
+                    const Item it = A.items[item];
+                    seed_t = stream_seed(A.seed, it.stream);
+                    p = it.draw0;
+                    left = it.n;
+                    dcand = 0;
+                    ddraw = 0;
+                    valid = left > 0;
+                }
+            }
+        }
+    }
+    Entry *out = A.lists + static_cast<size_t>(blockIdx.x) * A.kpad;
+    for (uint32_t i = tid; i < A.kpad; i += kThreads) out[i] = E[i];
+    for (int o = 16; o > 0; o >>= 1) {
+        screened += __shfl_down_sync(0xffffffffu, screened, o);
+        exact += __shfl_down_sync(0xffffffffu, exact, o);
+    }
+    if ((tid & 31) == 0) {
+        atomicAdd(&A.ctrl->screened, screened);
+        atomicAdd(&A.ctrl->exact_evals, exact);
+    }
+}
+
 // ---- 5. merge tree ------------------------------------------------------------------
 
 // Merge lists 2j and 2j+1 of `in` (nl lists of kpad entries, best first) into
@@ -973,8 +1136,15 @@ int context_init(Context &cx, int dev) {
 using ScreenFn = void (*)(ScreenArgs);
 
 ScreenFn screen_fn(bool fast_delta, bool filter) {
-    if (fast_delta) return filter ? screen_kernel<true, true> : screen_kernel<true, false>;
-    return filter ? screen_kernel<false, true> : screen_kernel<false, false>;
+    if (fast_delta) return filter ? screen_q_kernel<true> : screen_kernel<true, false>;
+    return filter ? screen_q_kernel<false> : screen_kernel<false, false>;
+}
+
+// Shared memory of the plain screen: the sort buffer, the elite table and,
+// in the filter form, the queue of candidates awaiting the exact order.
+size_t screen_smem(uint32_t sort_n, int ne, bool filter) {
+    return static_cast<size_t>(sort_n) * sizeof(Entry) + static_cast<size_t>(ne + 1) * kNtot * sizeof(float) +
+           (filter ? kPendCap * sizeof(Pend) : 0);
 }
 
 template <typename Fn>
@@ -1026,12 +1196,6 @@ __device__ __noinline__ double score64_at(const DevModel *m, const SynthConst *s
     (void)synth_score<kFastDelta, true, true>(*m, *sc, el, seed_t, p, h, g);
     return score64_genes(*m, g);
 }
-
-// A candidate waiting for its FP64 score (item-local index, draw offset).
-struct Pend {
-    uint32_t item, dcand, ddraw;
-};
-constexpr uint32_t kPendCap = 512;  // band queue per CTA
 
 // The screen in the precision form: the quadratic block of every candidate on
 // the tensor cores (two 128-thread groups, one MMA per group per round).
@@ -1332,8 +1496,9 @@ int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int
     if (tcf == (CSX_FLAG_TC_BF16 | CSX_FLAG_TC_FP16)) return CSX_ERR_BAD_ARGS;
     pl->tc = tcf != 0;
     pl->fp16 = tcf == CSX_FLAG_TC_FP16;
-    pl->smem = static_cast<size_t>(pl->sort_n) * sizeof(Entry) +
-               static_cast<size_t>(ne + 1) * kNtot * sizeof(float) + (pl->tc ? kTcSmemExtra : 0);
+    pl->smem = pl->tc ? static_cast<size_t>(pl->sort_n) * sizeof(Entry) +
+                            static_cast<size_t>(ne + 1) * kNtot * sizeof(float) + kTcSmemExtra
+                      : screen_smem(pl->sort_n, ne, pl->filter);
     if (pl->smem + 1024 > cx.max_smem) return CSX_ERR_LIMIT;
     if (grid_override > 0) {
         pl->grid = grid_override;
@@ -1756,8 +1921,7 @@ int plan_noalloc(const NoAllocDevice &dv, const csx_cfg &cfg, const csx_model &m
     pl->kpad = std::max<uint32_t>(32, pow2_at_least(cfg.keep));
     pl->sort_n = pow2_at_least(pl->kpad + 4ull * kThreads);
     pl->buf_cap = pl->sort_n - pl->kpad;
-    pl->smem = static_cast<size_t>(pl->sort_n) * sizeof(Entry) +
-               static_cast<size_t>(ne + 1) * kNtot * sizeof(float);
+    pl->smem = screen_smem(pl->sort_n, ne, pl->filter);
     if (pl->smem + 1024 > dv.max_smem) return CSX_ERR_LIMIT;
     int rc = screen_occupancy(screen_fn(pl->fast_delta, pl->filter), dv.num_sms, pl->smem, &pl->grid);
     if (rc) return rc;
