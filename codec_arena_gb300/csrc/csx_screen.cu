@@ -1285,13 +1285,33 @@ __global__ void __launch_bounds__(kThreads, 3) screen_tc_kernel(const __grid_con
         }
     };
 
+    // merge the buffer into the CTA's sorted list; publishes the threshold
+    auto merge = [&]() {
+        cta_sort_desc(E, A.sort_n);
+        for (uint32_t i = A.kpad + tid; i < A.sort_n; i += kThreads) E[i] = Entry{0ull, 0ull};
+        if (tid == 0) {
+            s_buf_n = 0;
+            const Entry kth = E[A.keep - 1];
+            if (kth.k1 != 0ull) {
+                s_t1 = kth.k1;
+                s_t2 = kth.k2;
+                const unsigned int ok = static_cast<unsigned int>(kth.k1 >> 32);
+                s_ts = okey_score(ok);
+                atomicMax(&A.ctrl->gtau, ok);
+            }
+        }
+        __syncthreads();
+    };
+
     for (;;) {
         __syncthreads();
         const unsigned int pn = min(s_pend_n, kPendCap);
         const int any = __syncthreads_or(valid || has_def);
         const int any_def = __syncthreads_or(has_def);
-        if (pn > 0 || any_def) {
-            // the buffer is empty here (it only fills from the queue, and every fill is sorted below)
+        // the queue is scored once it can employ every thread (or a thread
+        // waits on it, or the work is done); a flush appends <= pn + 256 <= 768
+        if (pn >= kThreads || any_def || (!any && pn > 0)) {
+            if (s_buf_n + kPendCap + kThreads > A.buf_cap) merge();  // make room first
             unsigned long long t1 = s_t1, t2 = s_t2;
             float ts = s_ts;
             const unsigned int g = *reinterpret_cast<volatile unsigned int *>(&A.ctrl->gtau);
@@ -1307,23 +1327,10 @@ __global__ void __launch_bounds__(kThreads, 3) screen_tc_kernel(const __grid_con
             }
             __syncthreads();
             if (tid == 0) s_pend_n = 0;
-            if (s_buf_n > 0) {
-                cta_sort_desc(E, A.sort_n);
-                for (uint32_t i = A.kpad + tid; i < A.sort_n; i += kThreads) E[i] = Entry{0ull, 0ull};
-                if (tid == 0) {
-                    s_buf_n = 0;
-                    const Entry kth = E[A.keep - 1];
-                    if (kth.k1 != 0ull) {
-                        s_t1 = kth.k1;
-                        s_t2 = kth.k2;
-                        const unsigned int ok = static_cast<unsigned int>(kth.k1 >> 32);
-                        s_ts = okey_score(ok);
-                        atomicMax(&A.ctrl->gtau, ok);
-                    }
-                }
-            }
             __syncthreads();
         }
+        const unsigned int bn = s_buf_n;
+        if (bn >= A.buf_cap / 2 || (!any && bn > 0)) merge();
         if (!any) break;
         unsigned long long t1 = s_t1;
         float ts = s_ts;
