@@ -2140,7 +2140,7 @@ struct BatchArgs {
     const IslandDev *isl;
     const unsigned int *base;  // n_islands + 1 prefix sums of the islands' item counts
     unsigned int *next_item;
-    uint32_t n_islands, sort_n;
+    uint32_t n_islands, sort_n, ne_max;
 };
 
 __global__ void batch_base_kernel(const IslandDev *__restrict__ isl, uint32_t n, unsigned int *__restrict__ base,
@@ -2180,6 +2180,7 @@ __global__ void __launch_bounds__(kThreads, 3) screen_batch_kernel(const __grid_
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Entry *E = reinterpret_cast<Entry *>(smem_raw);
     float *el = reinterpret_cast<float *>(E + B.sort_n);
+    Pend *pend = reinterpret_cast<Pend *>(el + (B.ne_max + 1) * kNtot);  // filter form: exact-order queue
     __shared__ RowModel s_m;
     __shared__ SynthConst s_sc;
     __shared__ unsigned int s_base[kMaxIslands + 1];
@@ -2187,7 +2188,7 @@ __global__ void __launch_bounds__(kThreads, 3) screen_batch_kernel(const __grid_
     __shared__ Ctrl *s_ctrl;
     __shared__ Entry *s_lists;
     __shared__ unsigned long long s_seed, s_t1, s_t2;
-    __shared__ unsigned int s_buf_n, s_next, s_keep, s_kpad, s_buf_cap;
+    __shared__ unsigned int s_buf_n, s_pend_n, s_next, s_keep, s_kpad, s_buf_cap;
     __shared__ int s_cur;
     __shared__ float s_ts, s_err;
 
@@ -2196,6 +2197,7 @@ __global__ void __launch_bounds__(kThreads, 3) screen_batch_kernel(const __grid_
     if (tid == 0) {
         s_cur = -1;
         s_buf_n = 0;
+        s_pend_n = 0;
         s_kpad = 0;
         s_keep = 0;
         s_buf_cap = 0;
@@ -2212,30 +2214,70 @@ __global__ void __launch_bounds__(kThreads, 3) screen_batch_kernel(const __grid_
     unsigned long long screened = 0, exact = 0;
     unsigned int gk = 0;
     uint32_t round = 0;
+    // a held entry: the buffer was full (exact-all form) or the queue was (filter form)
     bool has_def = false;
     Entry def{0ull, 0ull};
+    Pend pdef{0u, 0u, 0u};
+
+    // merge the buffer into the CTA's sorted list; publishes the island's threshold
+    auto merge = [&]() {
+        cta_sort_desc(E, B.sort_n);
+        for (uint32_t i = s_kpad + tid; i < B.sort_n; i += kThreads) E[i] = Entry{0ull, 0ull};
+        if (tid == 0) {
+            s_buf_n = 0;
+            const Entry kth = E[s_keep - 1];
+            if (kth.k1 != 0ull) {
+                s_t1 = kth.k1;
+                s_t2 = kth.k2;
+                const unsigned int ok = static_cast<unsigned int>(kth.k1 >> 32);
+                s_ts = okey_score(ok);
+                atomicMax(&s_ctrl->gtau, ok);
+            }
+        }
+        __syncthreads();
+    };
+    // reference-order score of a queued candidate; enters the buffer if it beats the threshold
+    auto rescore = [&](const Pend &q, unsigned long long t1, unsigned long long t2, float ts) {
+        const Item it = s_items[q.item];
+        const float s =
+            exact_score_isl<kFastDelta>(&s_m, &s_sc, el, stream_seed(s_seed, it.stream), it.draw0 + q.ddraw);
+        ++exact;
+        if (s >= ts) {
+            const unsigned long long k1 =
+                (static_cast<unsigned long long>(score_okey(s)) << 32) | static_cast<unsigned int>(~q.item);
+            const unsigned long long k2 = (static_cast<unsigned long long>(~q.dcand) << 32) | q.ddraw;
+            if (k1 > t1 || (k1 == t1 && k2 > t2)) E[s_kpad + atomicAdd(&s_buf_n, 1u)] = Entry{k1, k2};
+        }
+    };
 
     for (;;) {
         __syncthreads();
-        const unsigned int bn = s_buf_n;
+        const unsigned int pn = min(s_pend_n, kPendCap);
         const int any = __syncthreads_or(valid || has_def);
+        const int any_def = __syncthreads_or(has_def);
         const int cur = s_cur;
-        if (cur >= 0 && (bn >= s_buf_cap / 2 || (!any && bn > 0))) {
-            cta_sort_desc(E, B.sort_n);
-            for (uint32_t i = s_kpad + tid; i < B.sort_n; i += kThreads) E[i] = Entry{0ull, 0ull};
-            if (tid == 0) {
-                s_buf_n = 0;
-                const Entry kth = E[s_keep - 1];
-                if (kth.k1 != 0ull) {
-                    s_t1 = kth.k1;
-                    s_t2 = kth.k2;
-                    const unsigned int ok = static_cast<unsigned int>(kth.k1 >> 32);
-                    s_ts = okey_score(ok);
-                    atomicMax(&s_ctrl->gtau, ok);
-                }
+        if (kFilter && cur >= 0 && (pn >= kThreads || any_def || (!any && pn > 0))) {
+            // a flush appends <= pn + 256 <= 768 entries
+            if (s_buf_n + kPendCap + kThreads > s_buf_cap) merge();
+            unsigned long long t1 = s_t1, t2 = s_t2;
+            float ts = s_ts;
+            const unsigned int g = *reinterpret_cast<volatile unsigned int *>(&s_ctrl->gtau);
+            if ((static_cast<unsigned long long>(g) << 32) > t1) {
+                t1 = static_cast<unsigned long long>(g) << 32;
+                t2 = 0;
+                ts = okey_score(g);
+            }
+            for (uint32_t i = tid; i < pn; i += kThreads) rescore(pend[i], t1, t2, ts);
+            if (has_def) {
+                rescore(pdef, t1, t2, ts);
+                has_def = false;
             }
             __syncthreads();
+            if (tid == 0) s_pend_n = 0;
+            __syncthreads();
         }
+        const unsigned int bn = s_buf_n;
+        if (cur >= 0 && (bn >= s_buf_cap / 2 || (!any && bn > 0))) merge();
         if (!any) {
             if (cur >= 0) {  // publish this CTA's list and counts for the island it leaves
                 Entry *out = s_lists + static_cast<size_t>(blockIdx.x) * s_kpad;
@@ -2298,7 +2340,7 @@ __global__ void __launch_bounds__(kThreads, 3) screen_batch_kernel(const __grid_
         }
         const uint32_t kp = s_kpad, bcap = s_buf_cap;
         Entry *buf = E + kp;
-        if (has_def) {  // the merge above emptied the buffer: room for every held entry
+        if (!kFilter && has_def) {  // the merge above emptied the buffer: room for every held entry
             const unsigned int slot = atomicAdd(&s_buf_n, 1u);
             buf[slot] = def;
             has_def = false;
@@ -2319,18 +2361,22 @@ __global__ void __launch_bounds__(kThreads, 3) screen_batch_kernel(const __grid_
             asm volatile("" ::: "memory");
             const CandHead h = cand_head(s_sc, seed_t, p);
             float s;
-            if (kFilter) {
+            if (kFilter) {  // to the queue; scored in the reference order at the next flush
                 s = synth_score<kFastDelta, false, false>(s_m, s_sc, el, seed_t, p, h, nullptr);
                 if (s >= tlo) {
-                    s = exact_score_isl<kFastDelta>(&s_m, &s_sc, el, seed_t, p);
-                    ++exact;
-                } else {
-                    s = -INFINITY;
+                    const unsigned int slot = atomicAdd(&s_pend_n, 1u);
+                    if (slot < kPendCap) {
+                        pend[slot] = Pend{item, dcand, ddraw};
+                    } else {
+                        has_def = true;
+                        pdef = Pend{item, dcand, ddraw};
+                    }
                 }
+                s = -INFINITY;
             } else {
                 s = synth_score<kFastDelta, false>(s_m, s_sc, el, seed_t, p, h, nullptr);
             }
-            if (s >= ts) {
+            if (!kFilter && s >= ts) {
                 const unsigned long long k1 =
                     (static_cast<unsigned long long>(score_okey(s)) << 32) | static_cast<unsigned int>(~item);
                 const unsigned long long k2 = (static_cast<unsigned long long>(~dcand) << 32) | ddraw;
@@ -2458,7 +2504,7 @@ struct BatchLayout {
     std::vector<int> ne;
     std::vector<IslandBufs> b;
     bool fast = true, filter = true;
-    uint32_t sort_n = 0, kpad_max = 0, keep_max = 0;
+    uint32_t sort_n = 0, kpad_max = 0, keep_max = 0, ne_max = 0;
     size_t smem = 0;
     int grid = 0;
     IslandDev *d_isl = nullptr;
@@ -2503,7 +2549,8 @@ int batch_prepare(Context &cx, int n, const csx_cfg *cfgs, const csx_model *mode
         L->sort_n = std::max(L->sort_n, pow2_at_least(kpad + 4ull * kThreads));
         ne_max = std::max(ne_max, n_elites[i]);
     }
-    L->smem = static_cast<size_t>(L->sort_n) * sizeof(Entry) + static_cast<size_t>(ne_max + 1) * kNtot * sizeof(float);
+    L->ne_max = static_cast<uint32_t>(ne_max);
+    L->smem = screen_smem(L->sort_n, ne_max, L->filter);
     if (L->smem + 2048 > cx.max_smem) return CSX_ERR_LIMIT;
     BatchFn fn = batch_fn(L->fast, L->filter);
     CSX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(L->smem)));
@@ -2658,6 +2705,7 @@ int batch_enqueue(Context &cx, const BatchLayout &L, cudaStream_t st, bool captu
     B.next_item = L.d_next;
     B.n_islands = static_cast<uint32_t>(n);
     B.sort_n = L.sort_n;
+    B.ne_max = L.ne_max;
     batch_fn(L.fast, L.filter)<<<L.grid, kThreads, L.smem, st>>>(B);
     CSX_CUDA(cudaGetLastError());
     nk += 2;
