@@ -567,7 +567,7 @@ def main():
         except Exception:
             traffic = None
     roofline = {
-        "bound": "int-issue", "kernel": "csx::screen_kernel<true>",
+        "bound": "int-issue", "kernel": "csx::screen_q_kernel<true>",
         "achieved": achieved, "peak": peak, "unit": "Tlane-op/s",
         "frac": achieved / peak if peak else None, "traffic": traffic,
         "algorithmic_ops_per_candidate": LANE_OPS_PER_CAND,
