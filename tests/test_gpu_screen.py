@@ -362,3 +362,24 @@ def test_stream_range_errors():
         with pytest.raises(_lib.CsxError) as e:
             screen.screen(screen.Cfg(1000, 8, 1, threads=4), m, el, streams=rg)
         assert e.value.status == _lib.ERR_BAD_ARGS
+
+
+@pytest.mark.slow
+def test_makefile_screen_target(orc, tmp_path):
+    """The reference's `make screen` (Makefile:21-22): arena screen --model
+    state/surrogate.txt --elites pop/seed.txt --lambda 100000000 --keep 192
+    --seed 7 --threads 4, through this repository's CLI, equals the oracle's
+    promoted lines and count file."""
+    from codec_arena_gb300 import cli, genome, screen, workloads as wl
+
+    seed_pop = os.path.join(wl.GOLDEN_DIR, "pop_seed_96.txt")
+    out, cnt = tmp_path / "promoted.txt", tmp_path / "screens.txt"
+    rc = cli.main(["screen", "--model", wl.SURROGATE_161, "--elites", seed_pop, "--out", str(out),
+                   "--count-out", str(cnt), "--lambda", "100000000", "--keep", "192", "--seed", "7",
+                   "--threads", "4"])
+    assert rc == 0
+    assert cnt.read_text() == "100000000\n"
+    el = genome.load_elites(seed_pop)
+    want, n = _orc(orc, 100_000_000, 192, 7, 4, wl.surrogate_161(), el)
+    assert n == 100_000_000
+    assert out.read_text().splitlines(keepends=True) == [screen.format_survivor(r) for r in want]
