@@ -151,6 +151,7 @@ SIGNATURES.update({
                                        ctypes.POINTER(_int), ctypes.POINTER(CsxBatchTune), _vp, _vp, _vp]),
     "csx_last_batch_info": (_int, [ctypes.POINTER(CsxBatchInfo)]),
     "csx_tc_score": (_int, [ctypes.POINTER(CsxModel), _int, _vp, _i64, _int, _vp, _vp, _vp]),
+    "csx_score": (_int, [ctypes.POINTER(CsxModel), _vp, _i64, _int, _vp, _vp]),
 })
 TC_BF16, TC_FP16 = 1, 2
 

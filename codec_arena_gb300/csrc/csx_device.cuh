@@ -231,6 +231,30 @@ __device__ __forceinline__ float synth_score(const Model &M, const SynthConst &C
     return __fadd_rn(r, R);
 }
 
+// Model.score (src/screen.zig:97-112) of given genes, in the same f32 order as
+// synth_score's exact form: lane l holds w0 + wl_l g_l + sum_{i>=l} Wq[i][l]
+// (g_l g_i) accumulated row by row, the lanes are summed in order, then the
+// tail sum_{k>=16} wl_k g_k is added.
+__device__ __forceinline__ float score_genes_exact(const DevModel &M, const float (&g)[kNtot]) {
+    float S[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+#pragma unroll
+        for (int l = 0; l < k; ++l) S[l] = __fadd_rn(S[l], __fmul_rn(M.wq[tri(k, l)], __fmul_rn(g[l], g[k])));
+        S[k] = __fadd_rn(0.0f, __fmul_rn(M.wq[tri(k, k)], __fmul_rn(g[k], g[k])));
+    }
+    float R = 0.0f;
+#pragma unroll
+    for (int k = 16; k < kNtot; ++k) {
+        const float t = __fmul_rn(M.wlin[k], g[k]);
+        R = (k == 16) ? __fadd_rn(0.0f, t) : __fadd_rn(R, t);
+    }
+    float r = __fadd_rn(__fadd_rn(M.w0, __fmul_rn(M.wlin[0], g[0])), S[0]);
+#pragma unroll
+    for (int l = 1; l < 16; ++l) r = __fadd_rn(r, __fadd_rn(__fadd_rn(M.w0, __fmul_rn(M.wlin[l], g[l])), S[l]));
+    return __fadd_rn(r, R);
+}
+
 // Candidate-start walk: the start of the candidate after the one at p (the
 // immigrant test, then the jump test at the position it implies).
 __device__ __forceinline__ uint64_t walk_step2(const SynthConst &C, uint64_t seed_t, uint64_t p) {

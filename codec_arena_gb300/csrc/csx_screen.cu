@@ -3067,3 +3067,38 @@ extern "C" int csx_tc_score(const csx_model *model, int form, const float *d_gen
     CSX_CUDA(cudaGetLastError());
     return CSX_OK;
 }
+
+// ---- Model.score of given genomes ---------------------------------------------------
+namespace csx {
+
+__global__ void score_genes_kernel(const __grid_constant__ DevModel M, const float *__restrict__ genes, int64_t n,
+                                   int ldg, float *__restrict__ out) {
+    for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n;
+         r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        float g[kNtot];
+#pragma unroll
+        for (int k = 0; k < kNtot; ++k) g[k] = genes[r * ldg + k];
+        out[r] = score_genes_exact(M, g);
+    }
+}
+
+}  // namespace csx
+
+extern "C" int csx_score(const csx_model *model, const float *d_genes, int64_t n, int ldg, float *d_out,
+                         void *cuda_stream) {
+    if (!model || n < 0 || ldg < kNtot || (n > 0 && (!d_genes || !d_out))) return CSX_ERR_BAD_ARGS;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return CSX_ERR_NO_DEVICE;
+    }
+    if (n == 0) return CSX_OK;
+    int dev = 0, sms = 0;
+    CSX_CUDA(cudaGetDevice(&dev));
+    CSX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int grid = static_cast<int>(std::min<int64_t>((n + 255) / 256, 16ll * sms));
+    score_genes_kernel<<<grid, 256, 0, static_cast<cudaStream_t>(cuda_stream)>>>(make_dev_model(*model), d_genes, n,
+                                                                                   ldg, d_out);
+    CSX_CUDA(cudaGetLastError());
+    return CSX_OK;
+}

@@ -119,6 +119,19 @@ def screen(cfg: Cfg, model: Model, elites, streams: Optional[Tuple[int, int]] = 
     return out[: n_out.value], int(screened.value)
 
 
+def score_genes(model: Model, genes):
+    """Model.score (src/screen.zig:97-112) of the rows of a (n, >=29) float32
+    CUDA tensor, in the reference's f32 order, on the GPU."""
+    import torch
+
+    if not genes.is_cuda or genes.dtype != torch.float32 or genes.dim() != 2 or genes.stride(1) != 1:
+        raise TypeError("genes must be a 2-D float32 CUDA tensor with contiguous rows")
+    out = torch.empty(genes.shape[0], dtype=torch.float32, device=genes.device)
+    check(lib().csx_score(ctypes.byref(model.c), genes.data_ptr(), genes.shape[0], genes.stride(0), out.data_ptr(),
+                          torch.cuda.current_stream(genes.device).cuda_stream), "score")
+    return out
+
+
 def format_survivor(rec, flags: int = 0) -> str:
     """One promoted line (src/screen.zig:327-336 with FLAG_OUTPUT_29, else v6)."""
     buf = ctypes.create_string_buffer(1024)

@@ -254,6 +254,11 @@ int csx_screen_batch_device(int n_islands, const csx_cfg *cfgs, const csx_model 
 
 int csx_last_batch_info(csx_batch_info *out);
 
+/* Model.score (src/screen.zig:97-112) of n genomes given as rows of ldg >= 29
+ * device floats, in the reference's f32 operation order (the scores the screen
+ * ranks by), into d_out. Asynchronous on `cuda_stream`. */
+int csx_score(const csx_model *model, const float *d_genes, int64_t n, int ldg, float *d_out, void *cuda_stream);
+
 /* ---- precision form (tensor cores) -------------------------------------------
  * No counterpart in the reference, which scores in FP32 only. The quadratic
  * block over the 16 legacy genes runs on the tensor cores (tcgen05.mma, FP32

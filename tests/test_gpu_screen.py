@@ -383,3 +383,21 @@ def test_makefile_screen_target(orc, tmp_path):
     want, n = _orc(orc, 100_000_000, 192, 7, 4, wl.surrogate_161(), el)
     assert n == 100_000_000
     assert out.read_text().splitlines(keepends=True) == [screen.format_survivor(r) for r in want]
+
+
+def test_score_genes_in_reference_order(orc):
+    """csx_score equals the oracle's Model.score bit for bit, on random genes
+    and on genes with exact 0s and 1s."""
+    import torch
+
+    from codec_arena_gb300 import screen
+
+    rng = np.random.default_rng(71)
+    for w in _models().values():
+        m = screen.Model.from_compact(w)
+        om = orc.model_from_compact(w)
+        g = rng.random((3000, 29), dtype=np.float32)
+        g[::7] = np.round(g[::7])
+        got = screen.score_genes(m, torch.from_numpy(g).cuda()).cpu().numpy()
+        want = np.array([orc.score(om, row) for row in g], dtype=np.float32)
+        np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
