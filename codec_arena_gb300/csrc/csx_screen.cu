@@ -637,9 +637,9 @@ __device__ __noinline__ float exact_score_at(const ScreenArgs *__restrict__ A, c
     return synth_score<kFastDelta, false, true>(A->m, A->sc, el, seed_t, p, h, nullptr);
 }
 
-// kFilter: score with the FFMA filter form and evaluate the reference's f32
-// order only when the filter score is within A.err of the threshold.
-template <bool kFastDelta, bool kFilter>
+// The exact form (CSX_FLAG_EXACT_ALL, or a model whose filter bound is not
+// finite): every candidate scored in the reference's f32 order.
+template <bool kFastDelta>
 __global__ void __launch_bounds__(kThreads, 3) screen_kernel(const __grid_constant__ ScreenArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Entry *E = reinterpret_cast<Entry *>(smem_raw);
@@ -672,7 +672,7 @@ __global__ void __launch_bounds__(kThreads, 3) screen_kernel(const __grid_consta
         left = it.n;
         valid = left > 0;
     }
-    unsigned long long screened = 0, exact = 0;
+    unsigned long long screened = 0;
     unsigned int gk = 0;
     uint32_t round = 0;
     // An append that finds the buffer full is held here and the thread pauses
@@ -715,22 +715,10 @@ __global__ void __launch_bounds__(kThreads, 3) screen_kernel(const __grid_consta
             t2 = 0;
             ts = okey_score(gk);
         }
-        const float tlo = kFilter ? __fsub_rd(ts, A.err) : ts;
 #pragma unroll 1
         for (int r = 0; r < kRounds && valid && !has_def; ++r) {
             const CandHead h = cand_head(A.sc, seed_t, p);
-            float s;
-            if (kFilter) {
-                s = synth_score<kFastDelta, false, false>(A.m, A.sc, el, seed_t, p, h, nullptr);
-                if (s >= tlo) {
-                    s = exact_score_at<kFastDelta>(&A, el, seed_t, p);
-                    ++exact;
-                } else {
-                    s = -INFINITY;
-                }
-            } else {
-                s = synth_score<kFastDelta, false>(A.m, A.sc, el, seed_t, p, h, nullptr);
-            }
+            const float s = synth_score<kFastDelta, false>(A.m, A.sc, el, seed_t, p, h, nullptr);
             if (s >= ts) {
                 const unsigned long long k1 =
                     (static_cast<unsigned long long>(score_okey(s)) << 32) | static_cast<unsigned int>(~item);
@@ -769,14 +757,8 @@ __global__ void __launch_bounds__(kThreads, 3) screen_kernel(const __grid_consta
     Entry *out = A.lists + static_cast<size_t>(blockIdx.x) * A.kpad;
     for (uint32_t i = tid; i < A.kpad; i += kThreads) out[i] = E[i];
     // screened count: warp reduce then one atomic per warp
-    for (int o = 16; o > 0; o >>= 1) {
-        screened += __shfl_down_sync(0xffffffffu, screened, o);
-        exact += __shfl_down_sync(0xffffffffu, exact, o);
-    }
-    if ((tid & 31) == 0) {
-        atomicAdd(&A.ctrl->screened, screened);
-        if (kFilter) atomicAdd(&A.ctrl->exact_evals, exact);
-    }
+    for (int o = 16; o > 0; o >>= 1) screened += __shfl_down_sync(0xffffffffu, screened, o);
+    if ((tid & 31) == 0) atomicAdd(&A.ctrl->screened, screened);
 }
 
 // The filter form with the reference-order evaluation deferred: a candidate
@@ -1136,8 +1118,8 @@ int context_init(Context &cx, int dev) {
 using ScreenFn = void (*)(ScreenArgs);
 
 ScreenFn screen_fn(bool fast_delta, bool filter) {
-    if (fast_delta) return filter ? screen_q_kernel<true> : screen_kernel<true, false>;
-    return filter ? screen_q_kernel<false> : screen_kernel<false, false>;
+    if (fast_delta) return filter ? screen_q_kernel<true> : screen_kernel<true>;
+    return filter ? screen_q_kernel<false> : screen_kernel<false>;
 }
 
 // Shared memory of the plain screen: the sort buffer, the elite table and,
