@@ -48,7 +48,7 @@ def _compile(src: str, kind: str, verbose: bool) -> str:
     os.makedirs(BUILD, exist_ok=True)
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
     path = os.path.join(CSRC, src)
-    deps = [path, os.path.join(CSRC, "csx_device.cuh")] + [
+    deps = [path] + [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC)) if f.endswith(".cuh")] + [
         os.path.join(ROOT, "include", h) for h in ("csx_screen.h", "csx_surrogate.h", "csx_bench.h")]
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
         return obj
