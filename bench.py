@@ -292,6 +292,26 @@ def _fp64_scores(model, g):
 METRIC = "candidates/sec, 1 GB300: BF16-TC fused vs FP32 plain at top-256 recall>=0.999"
 
 
+def _measured_peaks() -> dict:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def hbm_ceiling(traffic_bytes, ms):
+    """DRAM bytes of one launch over its time, against the measured HBM copy
+    bandwidth (MEASURED_PEAKS.json hbm_gbs; else the 6.8 TB/s fallback)."""
+    pk = _measured_peaks().get("hbm_gbs")
+    src = "MEASURED_PEAKS.json hbm_gbs" if pk else "fallback 6.8 TB/s"
+    pk = pk or 6800.0
+    if not traffic_bytes or not ms:
+        return {"achieved": None, "peak": pk, "unit": "GB/s", "frac": None, "peak_source": src}
+    gbs = traffic_bytes / (ms * 1e-3) / 1e9
+    return {"achieved": gbs, "peak": pk, "unit": "GB/s", "frac": gbs / pk, "peak_source": src}
+
+
 def precision_forms(args, fp32_surv=None):
     """BF16 and FP16 tensor-core screens of the generation workload beside the
     plain FP32 screen: throughput (CUDA events, L2 flushed), top-K recall
@@ -332,6 +352,11 @@ def precision_forms(args, fp32_surv=None):
                      "screen_kernel_ms": statistics.mean(kms), "rescored": info["exact_evals"],
                      "screen_ctas": info["screen_ctas"],
                      "_surv": screen.survivors_from_bytes(d_out.cpu().numpy(), int(res[0]))}
+        if flag:  # tensor work of the form: one 128x16x16 MMA per 128 candidates = 512 flop per candidate
+            tf = 512.0 * args.lam / (statistics.mean(kms) * 1e-3) / 1e12
+            pk = _measured_peaks().get("bf16_tflops") or 1900.0
+            out[name]["tensor_roofline"] = {"achieved": tf, "peak": pk, "unit": "TFLOP/s", "frac": tf / pk,
+                                            "note": "the form stays bound by the integer synthesis"}
     if fp32_surv is not None:
         out["fp32_plain"] = {"_surv": fp32_surv}
     # FP64 ground truth: the exact screen's top 4096 rescored in FP64, certified complete below
@@ -578,6 +603,12 @@ def main():
                              if rates.get("splitmix64") else None},
         "issue_rates_measured": rates,
         "kernel_ms_per_launch": ms_screen,
+        # the other two ceilings, for completeness: HBM (the launch's DRAM
+        # traffic against the measured copy bandwidth) -- the kernel is far
+        # from it -- and the tensor cores, which the plain form does not use
+        "hbm": hbm_ceiling(traffic, ms_screen),
+        "tensor": {"achieved": 0.0, "unit": "TFLOP/s", "peak": _measured_peaks().get("bf16_tflops"),
+                   "frac": 0.0, "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)"},
     }
     line = {"metric": METRIC, "value": value, "unit": "candidates/s",
             "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
