@@ -35,6 +35,7 @@ struct IslandDev {
     unsigned long long *result;  // 4 words
     uint32_t keep, kpad, ne;
     float err;
+    JumpBound jb;
 };
 
 struct BatchArgs {
@@ -92,6 +93,7 @@ __global__ void __launch_bounds__(kThreads, 3) screen_batch_kernel(const __grid_
     __shared__ unsigned int s_buf_n, s_pend_n, s_next, s_keep, s_kpad, s_buf_cap;
     __shared__ int s_cur;
     __shared__ float s_ts, s_err;
+    __shared__ JumpBound s_jb;
 
     const uint32_t tid = threadIdx.x;
     for (uint32_t i = tid; i <= B.n_islands; i += kThreads) s_base[i] = B.base[i];
@@ -217,6 +219,7 @@ __global__ void __launch_bounds__(kThreads, 3) screen_batch_kernel(const __grid_
                 s_kpad = I->kpad;
                 s_buf_cap = B.sort_n - I->kpad;
                 s_err = I->err;
+                s_jb = I->jb;
                 s_cur = static_cast<int>(nx);
                 s_buf_n = 0;
                 s_t1 = 0;
@@ -264,7 +267,7 @@ __global__ void __launch_bounds__(kThreads, 3) screen_batch_kernel(const __grid_
             float s;
             if (kFilter) {  // to the queue; scored in the reference order at the next flush
                 s = synth_score<kFastDelta, false, false>(s_m, s_sc, el, seed_t, p, h, nullptr);
-                if (s >= tlo) {
+                if (s >= __fsub_rd(tlo, s_jb.c[h.jidx])) {
                     const unsigned int slot = atomicAdd(&s_pend_n, 1u);
                     if (slot < kPendCap) {
                         pend[slot] = Pend{item, dcand, ddraw};
@@ -543,6 +546,7 @@ int batch_prepare(Context &cx, int n, const csx_cfg *cfgs, const csx_model *mode
         d.kpad = std::max<uint32_t>(32, pow2_at_least(cfgs[i].keep));
         d.ne = static_cast<uint32_t>(n_elites[i]);
         d.err = filter_bound(models[i]);
+        jump_bound(models[i], &d.jb);
         out_off += cfgs[i].keep;
     }
     return CSX_OK;

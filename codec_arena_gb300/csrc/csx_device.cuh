@@ -34,6 +34,14 @@ struct DevModel {
     float wq[kNq];  // (i, j <= i) at i*(i+1)/2 + j  ==  Model.w_quad[i*16 + j]
 };
 
+// Bound on how far a jump can move the real score: with every gene in [0, 1],
+// setting gene j to another value in [0, 1] changes the surface by at most
+// c[j] = |w_lin[j]| + sum_i |Wq[i][j]| + sum_i |Wq[j][i]| (i != j) + |Wq[j][j]|
+// (rounded up). c[kNoJump] = 0, as are the unused entries.
+struct JumpBound {
+    float c[32];
+};
+
 // Per-call synthesis constants (uniform across the grid).
 struct SynthConst {
     uint64_t ne_magic;  // Lemire fastmod constant for ne
@@ -113,9 +121,12 @@ __device__ __forceinline__ uint32_t fastmod_u32(uint32_t x, uint64_t M, uint32_t
 }
 
 // Header of the candidate at draw position p (src/screen.zig:232-235,247-248).
+// A candidate without a jump carries jidx = kNoJump, past the last gene, so
+// that a 32-entry per-gene table (JumpBound) is indexed without a test.
+constexpr uint32_t kNoJump = 31;
 struct CandHead {
     uint32_t ea, eb;   // parent rows
-    uint32_t jidx;     // jump gene index, 0xFF when no jump
+    uint32_t jidx;     // jump gene index, kNoJump when no jump
     float jval;        // jump value
     bool imm;          // immigrant
     uint32_t len;      // draws the candidate consumes: 33/35/62/64
@@ -131,7 +142,7 @@ __device__ __forceinline__ CandHead cand_head(const SynthConst &C, uint64_t seed
     const bool jump = (draw_vh(sj) >> 8) < C.jump_thr;
     const uint32_t idx = draw_hi(sj + kGolden) % 29u;             // index drawn first
     h.jval = static_cast<float>(draw_vh(sj + 2 * kGolden) >> 8) * (1.0f / 16777216.0f);
-    h.jidx = jump ? idx : 0xFFu;
+    h.jidx = jump ? idx : kNoJump;
     h.len = (h.imm ? 33u : 62u) + (jump ? 2u : 0u);
     return h;
 }
@@ -159,6 +170,9 @@ __device__ __forceinline__ CandHead cand_head(const SynthConst &C, uint64_t seed
 // sum_{k>=16} w_k g_k (165 FFMA). Both orders are within gamma_n * A of the
 // real value (A = sum of |terms|), so the host bounds |fast - exact| and the
 // exact order is evaluated only for candidates the bound cannot rule out.
+// The filter form leaves the jump out (one compare and select per gene for
+// 2% of candidates): replacing gene j moves the real score by at most
+// JumpBound::c[j], which the caller adds to the bound.
 template <bool kFastDelta, bool kKeepGenes, bool kExact = true, class Model = DevModel>
 __device__ __forceinline__ float synth_score(const Model &M, const SynthConst &C,
                                              const float *__restrict__ el, uint64_t seed_t,
@@ -197,7 +211,9 @@ __device__ __forceinline__ float synth_score(const Model &M, const SynthConst &C
             g = fmaxf(fminf(g, 1.0f), 0.0f);
         else
             g = (g != g) ? 1.0f : fmaxf(fminf(g, 1.0f), 0.0f);
-        g = (static_cast<uint32_t>(k) == h.jidx) ? h.jval : g;
+        // The filter form scores the genome before the jump; the caller
+        // widens its threshold by JumpBound::c[h.jidx] instead.
+        if (kExact || kKeepGenes) g = (static_cast<uint32_t>(k) == h.jidx) ? h.jval : g;
         if (kKeepGenes) genes[k] = g;
         if (!kExact) {
             if (k < 16) {

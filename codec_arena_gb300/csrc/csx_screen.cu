@@ -138,6 +138,7 @@ struct Plan {
     bool filter = false;
     bool tc = false, fp16 = false;  // precision form (tensor cores + FP64 band)
     float err = 0.0f;
+    JumpBound jb{};  // widening of err for a candidate with a jump (filter mode)
 };
 
 int context_init(Context &cx, int dev) {
@@ -195,6 +196,21 @@ float filter_bound(const csx_model &m) {
     return std::nextafter(static_cast<float>(e), INFINITY);
 }
 
+// JumpBound of a model whose filter_bound is nonzero (finite weights): the
+// change of the real surface when gene j moves within [0, 1], computed in
+// double and rounded up with a 2^-20 relative margin.
+void jump_bound(const csx_model &m, JumpBound *jb) {
+    for (int j = 0; j < 32; ++j) jb->c[j] = 0.0f;
+    for (int j = 0; j < kNtot; ++j) {
+        double c = std::fabs(static_cast<double>(m.w_lin[j]));
+        if (j < 16)
+            for (int i = 0; i < 16; ++i)  // row j (i <= j) and column j (i > j) of the triangle
+                c += std::fabs(static_cast<double>(i <= j ? m.w_quad[j * 16 + i] : m.w_quad[i * 16 + j]));
+        c *= 1.0 + std::ldexp(1.0, -20);
+        jb->c[j] = c > 0.0 ? std::nextafter(static_cast<float>(c), INFINITY) : 0.0f;
+    }
+}
+
 // grid_override, item_cands, seg_cands: 0 = automatic (the batched screen
 // passes its own grid and the tuner's sizes).
 int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int ne, Plan *pl,
@@ -216,6 +232,7 @@ int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int
     pl->fast_delta = std::isfinite(cfg.sigma) && std::fabs(cfg.sigma) <= 1.0e38f &&
                      (cfg.sigma == 0.0f || std::fabs(cfg.sigma) >= 1.0e-30f);
     pl->err = filter_bound(model);
+    jump_bound(model, &pl->jb);
     pl->filter = !(cfg.flags & CSX_FLAG_EXACT_ALL) && pl->err > 0.0f;
 
     pl->kpad = std::max<uint32_t>(32, pow2_at_least(cfg.keep));
@@ -377,6 +394,7 @@ int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, cons
     A.sort_n = pl.sort_n;
     A.buf_cap = pl.buf_cap;
     A.err = pl.err;
+    A.jb = pl.jb;
     if (pl.tc) {
         TcScreenArgs P;
         P.A = A;
@@ -647,6 +665,7 @@ int plan_noalloc(const NoAllocDevice &dv, const csx_cfg &cfg, const csx_model &m
     pl->fast_delta = std::isfinite(cfg.sigma) && std::fabs(cfg.sigma) <= 1.0e38f &&
                      (cfg.sigma == 0.0f || std::fabs(cfg.sigma) >= 1.0e-30f);
     pl->err = filter_bound(model);
+    jump_bound(model, &pl->jb);
     pl->filter = !(cfg.flags & CSX_FLAG_EXACT_ALL) && pl->err > 0.0f;
     pl->kpad = std::max<uint32_t>(32, pow2_at_least(cfg.keep));
     pl->sort_n = pow2_at_least(pl->kpad + 4ull * kThreads);
@@ -773,6 +792,7 @@ int enqueue_screen_noalloc(const NoAllocDevice &dv, const csx_cfg &cfg, const cs
     A.sort_n = pl.sort_n;
     A.buf_cap = pl.buf_cap;
     A.err = pl.err;
+    A.jb = pl.jb;
     screen_fn(fast, pl.filter)<<<pl.grid, kThreads, pl.smem, st>>>(A);
     CSX_CUDA(cudaGetLastError());
     const size_t msmem = 2ull * pl.kpad * sizeof(Entry);

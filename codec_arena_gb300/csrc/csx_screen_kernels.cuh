@@ -19,6 +19,7 @@ struct ScreenArgs {
     Entry *lists;     // gridDim.x x kpad
     uint32_t keep, kpad, sort_n, buf_cap;
     float err;        // bound on |filter score - exact score| (filter mode)
+    JumpBound jb;     // added to err for a candidate with a jump (filter mode)
 };
 
 // Bitonic sort of E[0..n) (n a power of two), best entry first.
@@ -290,7 +291,7 @@ __global__ void __launch_bounds__(kThreads, 3) screen_q_kernel(const __grid_cons
         for (int r = 0; r < kRounds && valid && !has_def; ++r) {
             const CandHead h = cand_head(A.sc, seed_t, p);
             const float s = synth_score<kFastDelta, false, false>(A.m, A.sc, el, seed_t, p, h, nullptr);
-            if (s >= tlo) {
+            if (s >= __fsub_rd(tlo, A.jb.c[h.jidx])) {
                 const unsigned int slot = atomicAdd(&s_pend_n, 1u);
                 if (slot < kPendCap) {
                     pend[slot] = Pend{item, dcand, ddraw};
