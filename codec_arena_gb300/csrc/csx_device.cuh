@@ -280,6 +280,21 @@ __device__ __forceinline__ uint64_t walk_step2(const SynthConst &C, uint64_t see
     return p + (imm ? 33u : 62u) + (jump ? 2u : 0u);
 }
 
+// Length of the candidate whose start draw has state st = seed_t + (p + 1) *
+// kGolden: the immigrant test and the crossover candidate's jump test hashed
+// side by side, the immigrant's own jump test only when it is one.
+__device__ __forceinline__ uint32_t cand_len(const SynthConst &C, uint64_t st) {
+    const uint32_t vi = draw_vh(st + 2 * kGolden);
+    const uint32_t vj = draw_vh(st + 61 * kGolden);
+    uint32_t len = 62;
+    bool jump = (vj >> 8) < C.jump_thr;
+    if ((vi >> 8) < C.imm_thr) {
+        len = 33;
+        jump = (draw_vh(st + 32 * kGolden) >> 8) < C.jump_thr;
+    }
+    return len + (jump ? 2u : 0u);
+}
+
 // Order-preserving key of a score; -0 ranks with +0 and NaN below everything.
 __device__ __forceinline__ uint32_t score_okey(float x) {
     x = __fadd_rn(x, 0.0f);

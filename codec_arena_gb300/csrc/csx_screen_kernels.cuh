@@ -620,10 +620,12 @@ __global__ void __launch_bounds__(kThreads, 3) screen_tc_kernel(const __grid_con
             float R = 0.0f, x[16];
             uint32_t pk[8];
             uint32_t len = 0;
+            float jb = 0.0f;
             if (act) {
                 const CandHead h = cand_head(A.sc, seed_t, p);
                 synth_tc<kFastDelta, kFp16>(P.tm, A.sc, el, seed_t, p, h, R, x, pk);
                 len = h.len;
+                jb = A.jb.c[h.jidx];
             } else {
 #pragma unroll
                 for (int j = 0; j < 8; ++j) pk[j] = 0u;
@@ -636,7 +638,7 @@ __global__ void __launch_bounds__(kThreads, 3) screen_tc_kernel(const __grid_con
                 float s = R;
 #pragma unroll
                 for (int i = 0; i < 16; ++i) s = __fmaf_rn(x[i], y[i], s);
-                if (s >= tlo) {
+                if (s >= __fsub_rd(tlo, jb)) {
                     const unsigned int slot = atomicAdd(&s_pend_n, 1u);
                     if (slot < kPendCap) {
                         pend[slot] = Pend{item, dcand, ddraw};

@@ -178,7 +178,8 @@ namespace csx {
 // One candidate's genes exactly as synth_score makes them (src/screen.zig:
 // 225-250; same draws, same rounding), consumed for the precision form:
 // R = c + sum_k lin_k g_k (FP32 FMA), x = the 16 legacy genes (or 2g - 1 for
-// FP16), pk = x packed in pairs for the tensor-core tile.
+// FP16), pk = x packed in pairs for the tensor-core tile. The genes are the
+// candidate's before its jump, as in synth_score's filter form.
 template <bool kFastDelta, bool kFp16>
 __device__ __forceinline__ void synth_tc(const TcModel &T, const SynthConst &C, const float *__restrict__ el,
                                          uint64_t seed_t, uint64_t p, const CandHead &h, float &R, float (&x)[16],
@@ -211,7 +212,7 @@ __device__ __forceinline__ void synth_tc(const TcModel &T, const SynthConst &C, 
             g = __fadd_rn(par, __fmul_rn(__fadd_rn(y, nc), B));
             g = (g != g) ? 1.0f : fmaxf(fminf(g, 1.0f), 0.0f);
         }
-        g = (static_cast<uint32_t>(k) == h.jidx) ? h.jval : g;
+        // no jump here: the caller lowers the threshold by JumpBound::c[h.jidx]
         R = __fmaf_rn(T.lin[k], g, R);
         if (k < 16) x[k] = kFp16 ? __fmaf_rn(g, 2.0f, -1.0f) : g;
     }
