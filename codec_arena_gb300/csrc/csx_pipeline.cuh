@@ -202,6 +202,33 @@ __device__ __forceinline__ Run half_run(const SynthConst &C, uint64_t seed_t, ui
     return r;
 }
 
+// The same speculative run by the whole warp: lane j tests x + 62 j, the run
+// has up to 32 starts.
+__device__ __forceinline__ Run warp_run(const SynthConst &C, uint64_t seed_t, uint64_t x, int lane) {
+    const uint64_t pj = x + 62ull * static_cast<uint64_t>(lane);
+    const uint64_t s0 = seed_t + (pj + 1) * kGolden;
+    const bool imm = (draw_vh(s0 + 2 * kGolden) >> 8) < C.imm_thr;
+    const bool jb = (draw_vh(s0 + 61 * kGolden) >> 8) < C.jump_thr;
+    const uint32_t bn = __ballot_sync(0xffffffffu, imm || jb);
+    const uint32_t bi = __ballot_sync(0xffffffffu, imm);
+    Run r;
+    if (bn == 0) {
+        r.n = 32;
+        r.next = x + 62ull * 32;
+        return r;
+    }
+    const uint32_t f = static_cast<uint32_t>(__ffs(bn) - 1);
+    const uint64_t pf = x + 62ull * f;
+    uint32_t len = 64;
+    if ((bi >> f) & 1u) {
+        const bool ja = (draw_vh(seed_t + (pf + 33) * kGolden) >> 8) < C.jump_thr;
+        len = ja ? 35 : 33;
+    }
+    r.n = f + 1;
+    r.next = pf + len;
+    return r;
+}
+
 // Checkpoint (start of every D-th candidate) among the starts [k, k + cnt),
 // which lie at x + 62 (idx - k); D >= 64 > cnt, so at most one.
 __device__ __forceinline__ void record_ckpt(uint64_t *ckp, uint32_t ckcap, uint32_t dl, uint64_t k,
@@ -210,13 +237,20 @@ __device__ __forceinline__ void record_ckpt(uint64_t *ckp, uint32_t ckcap, uint3
     if (mk < k + cnt && (mk >> dl) < ckcap) ckp[mk >> dl] = x + 62ull * (mk - k);
 }
 
-// One warp per link of segment s and s+1 (same stream): s's chain from its
-// exit (lanes 0-15) and s+1's guess chain from its first draw (lanes 16-31)
-// advance together in speculative runs. Below M = the nearer of the two next
-// starts both chains' starts are known, and within a run they are 62 apart,
-// so the first shared start below M is y if (y - x) is a multiple of 62
-// inside x's run (or symmetrically). Otherwise both move to their first start
-// at or past M and the search goes on.
+// One warp per link of segment s and s+1 (same stream). Segment s's chain is
+// followed from its exit in whole-warp speculative runs until it lands on one
+// of the checkpoints the walk wrote for s+1's guess chain (every D-th start
+// before s+1's exit): a chain that reaches a start of another follows it from
+// there on, so the first checkpoint after the two chains meet is the first
+// one s's chain lands on, and only s's chain is walked. (Walking both chains
+// to their first shared start costs about four times the instructions.) If
+// s's chain passes the last of those checkpoints first, the meeting lies past
+// s+1's exit: the two chains then advance together, 16 lanes each, from s's
+// position and that checkpoint. Below M = the nearer of the two next starts
+// both chains' starts are known, and within a run they are 62 apart, so the
+// first shared start below M is y if (y - x) is a multiple of 62 inside x's
+// run (or symmetrically). Otherwise both move to their first start at or past
+// M and the search goes on.
 __global__ void link_kernel(SynthConst sc, StreamGeom g, SegRec *__restrict__ recs,
                             uint64_t *__restrict__ ck, Ctrl *__restrict__ ctrl) {
     const int lane = threadIdx.x & 31, half = lane >> 4, j = lane & 15;
@@ -229,11 +263,51 @@ __global__ void link_kernel(SynthConst sc, StreamGeom g, SegRec *__restrict__ re
     seg_of(g, s, t, c);
     const uint64_t seed_t = stream_seed(g.seed, t);
     uint64_t *ckp = ck + s * g.ckcap;
-    uint64_t x = r.merge_pos, k = r.n;                        // chain of segment s
-    uint64_t y = static_cast<uint64_t>(c + 1) * g.L, kb = 0;  // guess chain of s + 1
+    uint64_t x = r.merge_pos, k = r.n;  // chain of segment s
+    // s+1's walk checkpoints: starts m * D < n of s+1 (n is the walk's count;
+    // the link of s+1 rewrites that record with the same n)
+    const uint32_t n_next = *reinterpret_cast<volatile const uint32_t *>(&recs[s + 1].n);
+    const uint64_t *cky = ck + (s + 1) * g.ckcap;
+    const uint32_t D = 1u << g.d_log2;
+    const uint32_t mcap = min(g.ckcap, (n_next + D - 1) >> g.d_log2);  // >= 1: a chain has a start
+    uint32_t cm = 0;
+    uint64_t cy = cky[0];
+    while (cm + 1 < mcap && cy < x) cy = cky[++cm];
+    uint64_t y = cy, kb = static_cast<uint64_t>(cm) << g.d_log2;  // guess chain of s + 1
     uint64_t steps = 0;
     bool fail = false;
-    while (x != y) {
+    if (cy >= x) {
+        for (;;) {
+            const Run run = warp_run(sc, seed_t, x, lane);
+            const uint64_t d = cy - x;  // < one checkpoint gap + a run: fits 32 bits
+            const uint32_t dq = static_cast<uint32_t>(d) / 62u;
+            if (static_cast<uint32_t>(d) == dq * 62u && dq < run.n) {  // lands on it
+                if (lane == 0) record_ckpt(ckp, g.ckcap, g.d_log2, k, dq, x);
+                k += dq;
+                x = cy;
+                break;
+            }
+            if (lane == 0) record_ckpt(ckp, g.ckcap, g.d_log2, k, run.n, x);
+            k += run.n;
+            x = run.next;
+            steps += run.n;
+            while (cy < x && cm + 1 < mcap) cy = cky[++cm];
+            if (cy < x) {  // past the last checkpoint: meet beyond it (below)
+                y = cy;
+                kb = static_cast<uint64_t>(cm) << g.d_log2;
+                break;
+            }
+            if (steps > kLinkCap) {
+                fail = true;
+                break;
+            }
+        }
+        if (x == cy) {
+            y = cy;
+            kb = static_cast<uint64_t>(cm) << g.d_log2;
+        }
+    }
+    while (x != y && !fail) {
         const Run mine = half_run(sc, seed_t, half ? y : x, j, half);
         Run rx, ry;
         rx.n = __shfl_sync(0xffffffffu, mine.n, 0);
