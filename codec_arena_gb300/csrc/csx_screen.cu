@@ -686,7 +686,7 @@ int plan_noalloc(const NoAllocDevice &dv, const csx_cfg &cfg, const csx_model &m
     uint64_t gran = 2;
     if ((it == 0 || it == (1u << 24)) && (jt == 0 || jt == (1u << 24)))
         gran = (it ? 33 : 62) + (jt ? 2 : 0);
-    uint64_t L = 64 * std::min<uint64_t>(kDefaultSegCands, my_max);
+    uint64_t L = 64 * std::min<uint64_t>(kNoAllocSegCands, my_max);
     L = ((L + gran - 1) / gran) * gran;
     g.L = L;
     g.C = static_cast<uint32_t>(std::max<uint64_t>(1, (64 * g.per + L - 1) / L));
