@@ -131,6 +131,23 @@ def test_segment_linking(orc, env, seg, item):
     check(orc, 7_001, 20, 1, 3, wl.seeded_normal_model(), wl.seeded_elites(5), imm=0.3, jump=0.4)
 
 
+@pytest.mark.parametrize("seg", [1, 3, 37, 300])
+def test_every_candidate_once(orc, env, seg):
+    """keep = lambda: every candidate survives, so the survivor list is the
+    whole generation. Segments of a few candidates make nearly every
+    boundary meet past the next segment's walk checkpoints, and the items of
+    64 candidates split every segment's range: each candidate must appear
+    once, with its stream, index, draw, parents and genes."""
+    from codec_arena_gb300 import workloads as wl
+
+    env.setenv("CSX_SEG_CANDS", str(seg))
+    env.setenv("CSX_ITEM_CANDS", "64")
+    got = check(orc, 4096, 4096, 31, 2, wl.surrogate_161(), wl.seeded_elites(16), imm=0.2, jump=0.3)
+    assert len(got) == 4096
+    keys = {(int(r["stream"]), int(r["index"])) for r in got}
+    assert keys == {(t, i) for t in range(2) for i in range(2048)}
+
+
 @pytest.mark.parametrize("imm,jump", [(0.0, 0.0), (1.0, 0.0), (1.0, 1.0), (0.0, 1.0), (0.0, 0.02),
                                       (0.5, 0.5), (0.01, 0.0), (1e-7, 0.02), (float("nan"), 2.0)])
 def test_branch_probabilities(orc, env, imm, jump):
