@@ -328,6 +328,21 @@ def hbm_ceiling(traffic_bytes, ms):
     return {"achieved": gbs, "peak": pk, "unit": "GB/s", "frac": gbs / pk, "peak_source": src}
 
 
+def issue_slots(achieved_tops, clocks):
+    """The algorithmic lane-ops/s against the GPU's instruction issue limit:
+    one warp instruction per scheduler per clock, 4 schedulers per SM, at the
+    SM clock sampled during the timed region (its maximum if none)."""
+    import torch
+
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
+    if not mhz:
+        return {"achieved": achieved_tops, "peak": None, "unit": "Tlane-op/s", "frac": None}
+    peak = 4 * 32 * sms * mhz * 1e6 / 1e12
+    return {"achieved": achieved_tops, "peak": peak, "unit": "Tlane-op/s", "frac": achieved_tops / peak,
+            "peak_source": f"issue limit: 4 schedulers x 32 lanes x {sms} SMs x {mhz:.0f} MHz"}
+
+
 def precision_forms(args, fp32_surv=None):
     """BF16 and FP16 tensor-core screens of the generation workload beside the
     plain FP32 screen: throughput (CUDA events, L2 flushed), top-K recall
@@ -619,6 +634,7 @@ def main():
                              "frac": (cand_s_kernel * DRAWS_PER_CAND / rates["splitmix64"])
                              if rates.get("splitmix64") else None},
         "issue_rates_measured": rates,
+        "issue_slots": issue_slots(achieved, clocks),
         "kernel_ms_per_launch": ms_screen,
         # the other two ceilings, for completeness: HBM (the launch's DRAM
         # traffic against the measured copy bandwidth) -- the kernel is far
