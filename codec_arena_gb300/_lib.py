@@ -155,6 +155,22 @@ SIGNATURES.update({
 })
 TC_BF16, TC_FP16 = 1, 2
 
+FULL_NF = 465  # compact length of the full quadratic surface (csx_screen.h)
+
+
+class CsxModelFull(ctypes.Structure):
+    _fields_ = [("w0", _f32), ("w_lin", _f32 * NTOT), ("w_quad", _f32 * 435)]
+
+
+SIGNATURES.update({
+    "csx_model_full_from_compact": (_int, [ctypes.POINTER(_f32), _int, ctypes.POINTER(CsxModelFull)]),
+    "csx_screen_full": (_int, [ctypes.POINTER(CsxCfg), ctypes.POINTER(CsxModelFull), _vp, _int, _vp, _u64,
+                               ctypes.POINTER(_u64), ctypes.POINTER(_u64)]),
+    "csx_screen_full_device": (_int, [ctypes.POINTER(CsxCfg), ctypes.POINTER(CsxModelFull), _vp, _int, _vp,
+                                      _u64, _vp, _vp]),
+    "csx_score_full": (_int, [ctypes.POINTER(CsxModelFull), _vp, _i64, _int, _vp, _vp]),
+})
+
 SG_FP32, SG_BF16, SG_FP64 = 0, 1, 2
 
 _lib = None

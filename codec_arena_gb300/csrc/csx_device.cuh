@@ -27,6 +27,18 @@ constexpr int kNtot = 29;
 constexpr int kNq = 136;  // lower-triangular quad terms over the 16 legacy genes
 
 // Model in the compact triangular form used on the device.
+// The full quadratic surface over all 29 genes (no reference code: the
+// extension docs/RESEARCH_V05C.md:99-102 queues). Its f32 score is defined
+// by one FMA order, r = w0; t_k = fma chain of w_lin[k] + sum_{l<=k} Q_kl g_l;
+// r = fma(g_k, t_k, r) for k = 0..28 -- the order synth_full evaluates while
+// the genes are synthesised, and the oracle's orc_score_full.
+constexpr int kNqFull = kNtot * (kNtot + 1) / 2;  // 435
+struct FullModel {
+    float w0;
+    float wlin[kNtot];
+    float wq[kNqFull];  // (i, j <= i) at i*(i+1)/2 + j
+};
+
 struct DevModel {
     float w0;
     float w16;  // 16 * w0 (exact): the intercept as Model.score counts it
@@ -245,6 +257,66 @@ __device__ __forceinline__ float synth_score(const Model &M, const SynthConst &C
     for (int l = 1; l < 16; ++l)
         r = __fadd_rn(r, __fadd_rn(__fadd_rn(m_w0(M), __fmul_rn(m_lin(M, l), G[l])), S[l]));
     return __fadd_rn(r, R);
+}
+
+// One candidate scored on the full surface (FullModel's FMA order), the
+// synthesis exactly as synth_score's: genes in registers, the jump applied.
+template <bool kFastDelta, bool kKeepGenes>
+__device__ __forceinline__ float synth_full(const FullModel &M, const SynthConst &C,
+                                            const float *__restrict__ el, uint64_t seed_t, uint64_t p,
+                                            const CandHead &h, float *genes) {
+    const uint64_t s0 = seed_t + (p + 1) * kGolden;
+    const uint32_t ra = h.imm ? C.ne : h.ea;
+    const uint32_t rb = h.imm ? C.ne : h.eb;
+    const float *pa = el + ra * kNtot;
+    const float *pb = el + rb * kNtot;
+    const float B = h.imm ? 0.5f : C.sigma;
+    const float nb1 = h.imm ? -0.5f : C.nsig1;
+    const float B23 = h.imm ? 0x1p-24f : C.sigma23;
+    const uint64_t step = h.imm ? kGolden : 2 * kGolden;
+    uint64_t su = s0 + (h.imm ? 3ull : 4ull) * kGolden;
+
+    float G[kNtot];
+    float R = M.w0;
+#pragma unroll
+    for (int k = 0; k < kNtot; ++k) {
+        const uint32_t bw = draw_bitword(su - kGolden);
+        const uint32_t vh = draw_vh(su);
+        su += step;
+        const float *src = (static_cast<int32_t>(bw) < 0) ? pb : pa;
+        const float par = src[k];
+        float g;
+        if (kFastDelta) {
+            g = __fadd_rn(par, __fmaf_rn(__uint2float_rn(vh >> 8), B23, nb1));
+            g = fmaxf(fminf(g, 1.0f), 0.0f);
+        } else {
+            const float y = __uint_as_float(((vh >> 8) & 0x7FFFFFu) | 0x3F800000u);
+            const float nc = (static_cast<int32_t>(vh) < 0) ? -1.0f : -2.0f;
+            g = __fadd_rn(par, __fmul_rn(__fadd_rn(y, nc), B));
+            g = (g != g) ? 1.0f : fmaxf(fminf(g, 1.0f), 0.0f);
+        }
+        g = (static_cast<uint32_t>(k) == h.jidx) ? h.jval : g;
+        if (kKeepGenes) genes[k] = g;
+        G[k] = g;
+        float t = M.wlin[k];
+#pragma unroll
+        for (int l = 0; l <= k; ++l) t = __fmaf_rn(M.wq[tri(k, l)], G[l], t);
+        R = __fmaf_rn(g, t, R);
+    }
+    return R;
+}
+
+// The full surface's score of given genes, in synth_full's order.
+__device__ __forceinline__ float score_full(const FullModel &M, const float (&g)[kNtot]) {
+    float R = M.w0;
+#pragma unroll
+    for (int k = 0; k < kNtot; ++k) {
+        float t = M.wlin[k];
+#pragma unroll
+        for (int l = 0; l <= k; ++l) t = __fmaf_rn(M.wq[tri(k, l)], g[l], t);
+        R = __fmaf_rn(g[k], t, R);
+    }
+    return R;
 }
 
 // Model.score (src/screen.zig:97-112) of given genes, in the same f32 order as

@@ -161,6 +161,20 @@ ScreenFn screen_fn(bool fast_delta, bool filter) {
     return filter ? screen_q_kernel<false> : screen_kernel<false>;
 }
 
+using FullScreenFn = void (*)(FullScreenArgs);
+
+FullScreenFn screen_full_fn(bool fast_delta) {
+    return fast_delta ? screen_kernel<true, FullScreenArgs> : screen_kernel<false, FullScreenArgs>;
+}
+
+FullModel make_full_model(const csx_model_full &m) {
+    FullModel f;
+    f.w0 = m.w0;
+    for (int k = 0; k < kNtot; ++k) f.wlin[k] = m.w_lin[k];
+    for (int q = 0; q < kNqFull; ++q) f.wq[q] = m.w_quad[q];
+    return f;
+}
+
 // Shared memory of the plain screen: the sort buffer, the elite table and,
 // in the filter form, the queue of candidates awaiting the exact order.
 size_t screen_smem(uint32_t sort_n, int ne, bool filter) {
@@ -215,7 +229,7 @@ void jump_bound(const csx_model &m, JumpBound *jb) {
 // passes its own grid and the tuner's sizes).
 int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int ne, Plan *pl,
               int grid_override = 0, uint64_t item_cands = 0, uint64_t seg_cands = 0, uint64_t t_begin = 0,
-              uint64_t t_end = 0) {
+              uint64_t t_end = 0, const csx_model_full *full = nullptr) {
     StreamGeom &g = pl->g;
     g.seed = cfg.seed;
     g.T = std::max<uint64_t>(1, std::min<uint64_t>(cfg.threads, cfg.lambda));  // src/screen.zig:267
@@ -233,13 +247,14 @@ int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int
                      (cfg.sigma == 0.0f || std::fabs(cfg.sigma) >= 1.0e-30f);
     pl->err = filter_bound(model);
     jump_bound(model, &pl->jb);
-    pl->filter = !(cfg.flags & CSX_FLAG_EXACT_ALL) && pl->err > 0.0f;
+    pl->filter = !full && !(cfg.flags & CSX_FLAG_EXACT_ALL) && pl->err > 0.0f;
 
     pl->kpad = std::max<uint32_t>(32, pow2_at_least(cfg.keep));
     pl->sort_n = pow2_at_least(pl->kpad + 4ull * kThreads);
     pl->buf_cap = pl->sort_n - pl->kpad;
     const uint32_t tcf = cfg.flags & (CSX_FLAG_TC_BF16 | CSX_FLAG_TC_FP16);
     if (tcf == (CSX_FLAG_TC_BF16 | CSX_FLAG_TC_FP16)) return CSX_ERR_BAD_ARGS;
+    if (full && tcf) return CSX_ERR_BAD_ARGS;  // the precision form scores the reference surface
     pl->tc = tcf != 0;
     pl->fp16 = tcf == CSX_FLAG_TC_FP16;
     pl->smem = pl->tc ? static_cast<size_t>(pl->sort_n) * sizeof(Entry) +
@@ -256,6 +271,9 @@ int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int
         int rc = screen_occupancy(screen_tc_fn(pl->fast_delta, pl->fp16), cx.num_sms, pl->smem, &pl->grid);
         if (rc) return rc;
         pl->grid = kTcCtasPerSm * cx.num_sms;
+    } else if (full) {
+        int rc = screen_occupancy(screen_full_fn(pl->fast_delta), cx.num_sms, pl->smem, &pl->grid);
+        if (rc) return rc;
     } else {
         int rc = screen_occupancy(screen_fn(pl->fast_delta, pl->filter), cx.num_sms, pl->smem, &pl->grid);
         if (rc) return rc;
@@ -299,9 +317,9 @@ int unit_blocks(uint64_t n, int threads) { return static_cast<int>((n + threads 
 // Enqueue the whole pipeline on `st`. Device inputs: genomes (csx_genome x ne).
 int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, const csx_genome *d_genomes,
                    int ne, csx_survivor *d_out, unsigned long long *d_result, cudaStream_t st,
-                   uint64_t t_begin = 0, uint64_t t_end = 0) {
+                   uint64_t t_begin = 0, uint64_t t_end = 0, const csx_model_full *full = nullptr) {
     Plan pl;
-    int rc = make_plan(cx, cfg, model, ne, &pl, 0, 0, 0, t_begin, t_end);
+    int rc = make_plan(cx, cfg, model, ne, &pl, 0, 0, 0, t_begin, t_end, full);
     if (rc) return rc;
     const StreamGeom &g = pl.g;
     const bool fast = pl.fast_delta;
@@ -405,6 +423,11 @@ int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, cons
         rc = tc_error_bound(model, pl.fp16, &P.err_abs);
         if (rc) return rc;
         screen_tc_fn(fast, pl.fp16)<<<pl.grid, kThreads, pl.smem, st>>>(P);
+    } else if (full) {
+        FullScreenArgs F;
+        static_cast<ScreenArgs &>(F) = A;
+        F.fm = make_full_model(*full);
+        screen_full_fn(fast)<<<pl.grid, kThreads, pl.smem, st>>>(F);
     } else {
         screen_fn(fast, pl.filter)<<<pl.grid, kThreads, pl.smem, st>>>(A);
     }
@@ -427,7 +450,15 @@ int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, cons
         n = m;
     }
     CSX_CUDA(mark(4));
-    if (pl.tc && fast)
+    if (full) {
+        FullScreenArgs F;
+        static_cast<ScreenArgs &>(F) = A;
+        F.fm = make_full_model(*full);
+        if (fast)
+            regen_full_kernel<true><<<unit_blocks(cfg.keep, 128), 128, 0, st>>>(F, cur, ids, tribes, d_out);
+        else
+            regen_full_kernel<false><<<unit_blocks(cfg.keep, 128), 128, 0, st>>>(F, cur, ids, tribes, d_out);
+    } else if (pl.tc && fast)
         regen64_kernel<true><<<unit_blocks(cfg.keep, 128), 128, 0, st>>>(A, cur, ids, tribes, d_out);
     else if (pl.tc)
         regen64_kernel<false><<<unit_blocks(cfg.keep, 128), 128, 0, st>>>(A, cur, ids, tribes, d_out);
@@ -498,8 +529,13 @@ int csx_limits(uint64_t *max_keep, uint64_t *max_elites) {
     return CSX_OK;
 }
 
-int csx_screen_device(const csx_cfg *cfg, const csx_model *model, const csx_genome *d_elites, int n_elites,
-                      csx_survivor *d_out, uint64_t out_cap, uint64_t *d_result, void *cuda_stream) {
+}  // extern "C"
+
+namespace csx {
+
+int screen_device(const csx_cfg *cfg, const csx_model *model, const csx_genome *d_elites, int n_elites,
+                  csx_survivor *d_out, uint64_t out_cap, uint64_t *d_result, void *cuda_stream,
+                  const csx_model_full *full) {
     int rc = check_common(cfg, model, n_elites);
     if (rc) return rc;
     if (!d_elites || !d_result || (!d_out && cfg->lambda > 0)) return CSX_ERR_BAD_ARGS;
@@ -521,7 +557,34 @@ int csx_screen_device(const csx_cfg *cfg, const csx_model *model, const csx_geno
     }
     csx_cfg c = *cfg;
     return enqueue_screen(*cx, c, *model, d_elites, n_elites, d_out,
-                          reinterpret_cast<unsigned long long *>(d_result), st);
+                          reinterpret_cast<unsigned long long *>(d_result), st, 0, 0, full);
+}
+
+const csx_model kZeroModel{};  // the reference surface's slot when the full surface scores
+
+}  // namespace csx
+
+extern "C" {
+
+int csx_screen_device(const csx_cfg *cfg, const csx_model *model, const csx_genome *d_elites, int n_elites,
+                      csx_survivor *d_out, uint64_t out_cap, uint64_t *d_result, void *cuda_stream) {
+    return screen_device(cfg, model, d_elites, n_elites, d_out, out_cap, d_result, cuda_stream, nullptr);
+}
+
+int csx_model_full_from_compact(const float *w, int n, csx_model_full *out) {
+    if (!w || !out) return CSX_ERR_BAD_ARGS;
+    if (n != CSX_FULL_NF) return CSX_ERR_BAD_MODEL;
+    out->w0 = w[0];
+    for (int k = 0; k < kNtot; ++k) out->w_lin[k] = w[1 + k];
+    for (int q = 0; q < kNqFull; ++q) out->w_quad[q] = w[1 + kNtot + q];
+    return CSX_OK;
+}
+
+int csx_screen_full_device(const csx_cfg *cfg, const csx_model_full *model, const csx_genome *d_elites,
+                           int n_elites, csx_survivor *d_out, uint64_t out_cap, uint64_t *d_result,
+                           void *cuda_stream) {
+    if (!model) return CSX_ERR_BAD_ARGS;
+    return screen_device(cfg, &kZeroModel, d_elites, n_elites, d_out, out_cap, d_result, cuda_stream, model);
 }
 
 }  // extern "C"
@@ -531,7 +594,7 @@ namespace csx {
 // csx_screen / csx_screen_range: host buffers, a private stream, synchronous.
 int screen_host(const csx_cfg *cfg, const csx_model *model, const csx_genome *elites, int n_elites,
                 uint64_t t_begin, uint64_t t_end, csx_survivor *out, uint64_t out_cap, uint64_t *n_out,
-                uint64_t *screened) {
+                uint64_t *screened, const csx_model_full *full = nullptr) {
     if (n_out) *n_out = 0;
     if (screened) *screened = 0;
     int rc = check_common(cfg, model, n_elites);
@@ -560,7 +623,7 @@ int screen_host(const csx_cfg *cfg, const csx_model *model, const csx_genome *el
     cudaError_t e = cudaMemcpyAsync(dg, elites, static_cast<size_t>(n_elites) * sizeof(csx_genome),
                                     cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) {
-        rc = enqueue_screen(*cx, *cfg, *model, dg, n_elites, ds, dr, st, t_begin, t_end);
+        rc = enqueue_screen(*cx, *cfg, *model, dg, n_elites, ds, dr, st, t_begin, t_end, full);
         if (rc == CSX_OK) {
             e = cudaMemcpyAsync(res, dr, sizeof(res), cudaMemcpyDeviceToHost, st);
             if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -594,6 +657,16 @@ extern "C" {
 int csx_screen(const csx_cfg *cfg, const csx_model *model, const csx_genome *elites, int n_elites,
                csx_survivor *out, uint64_t out_cap, uint64_t *n_out, uint64_t *screened) {
     return screen_host(cfg, model, elites, n_elites, 0, 0, out, out_cap, n_out, screened);
+}
+
+int csx_screen_full(const csx_cfg *cfg, const csx_model_full *model, const csx_genome *elites, int n_elites,
+                    csx_survivor *out, uint64_t out_cap, uint64_t *n_out, uint64_t *screened) {
+    if (!model) {
+        if (n_out) *n_out = 0;
+        if (screened) *screened = 0;
+        return CSX_ERR_BAD_ARGS;
+    }
+    return screen_host(cfg, &kZeroModel, elites, n_elites, 0, 0, out, out_cap, n_out, screened, model);
 }
 
 int csx_screen_range(const csx_cfg *cfg, const csx_model *model, const csx_genome *elites, int n_elites,
@@ -864,7 +937,37 @@ __global__ void score_genes_kernel(const __grid_constant__ DevModel M, const flo
     }
 }
 
+__global__ void score_full_kernel(const __grid_constant__ FullModel M, const float *__restrict__ genes, int64_t n,
+                                  int ldg, float *__restrict__ out) {
+    for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n;
+         r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        float g[kNtot];
+#pragma unroll
+        for (int k = 0; k < kNtot; ++k) g[k] = genes[r * ldg + k];
+        out[r] = score_full(M, g);
+    }
+}
+
 }  // namespace csx
+
+extern "C" int csx_score_full(const csx_model_full *model, const float *d_genes, int64_t n, int ldg, float *d_out,
+                              void *cuda_stream) {
+    if (!model || n < 0 || ldg < kNtot || (n > 0 && (!d_genes || !d_out))) return CSX_ERR_BAD_ARGS;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return CSX_ERR_NO_DEVICE;
+    }
+    if (n == 0) return CSX_OK;
+    int dev = 0, sms = 0;
+    CSX_CUDA(cudaGetDevice(&dev));
+    CSX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int grid = static_cast<int>(std::min<int64_t>((n + 255) / 256, 16ll * sms));
+    score_full_kernel<<<grid, 256, 0, static_cast<cudaStream_t>(cuda_stream)>>>(make_full_model(*model), d_genes, n,
+                                                                                  ldg, d_out);
+    CSX_CUDA(cudaGetLastError());
+    return CSX_OK;
+}
 
 extern "C" int csx_score(const csx_model *model, const float *d_genes, int64_t n, int ldg, float *d_out,
                          void *cuda_stream) {

@@ -22,6 +22,37 @@ struct ScreenArgs {
     JumpBound jb;     // added to err for a candidate with a jump (filter mode)
 };
 
+// The screen on the full quadratic surface: the same pipeline, the
+// candidates scored by synth_full (no filter: its FMA order is the defined
+// score).
+struct FullScreenArgs : ScreenArgs {
+    FullModel fm;
+};
+
+// The score of the candidate at p (header h) under the call's surface.
+template <bool kFastDelta>
+__device__ __forceinline__ float cand_score(const ScreenArgs &A, const float *el, uint64_t seed_t, uint64_t p,
+                                            const CandHead &h) {
+    return synth_score<kFastDelta, false>(A.m, A.sc, el, seed_t, p, h, nullptr);
+}
+template <bool kFastDelta>
+__device__ __forceinline__ float cand_score(const FullScreenArgs &A, const float *el, uint64_t seed_t,
+                                            uint64_t p, const CandHead &h) {
+    return synth_full<kFastDelta, false>(A.fm, A.sc, el, seed_t, p, h, nullptr);
+}
+
+// The same with the genes kept (regeneration of survivors).
+template <bool kFastDelta>
+__device__ __forceinline__ float cand_genes(const DevModel &m, const SynthConst &sc, const float *el,
+                                            uint64_t seed_t, uint64_t p, const CandHead &h, float *genes) {
+    return synth_score<kFastDelta, true>(m, sc, el, seed_t, p, h, genes);
+}
+template <bool kFastDelta>
+__device__ __forceinline__ float cand_genes(const FullModel &m, const SynthConst &sc, const float *el,
+                                            uint64_t seed_t, uint64_t p, const CandHead &h, float *genes) {
+    return synth_full<kFastDelta, true>(m, sc, el, seed_t, p, h, genes);
+}
+
 // Bitonic sort of E[0..n) (n a power of two), best entry first.
 __device__ void cta_sort_desc(Entry *E, uint32_t n) {
     for (uint32_t size = 2; size <= n; size <<= 1) {
@@ -52,9 +83,10 @@ __device__ __noinline__ float exact_score_at(const ScreenArgs *__restrict__ A, c
 }
 
 // The exact form (CSX_FLAG_EXACT_ALL, or a model whose filter bound is not
-// finite): every candidate scored in the reference's f32 order.
-template <bool kFastDelta>
-__global__ void __launch_bounds__(kThreads, 3) screen_kernel(const __grid_constant__ ScreenArgs A) {
+// finite): every candidate scored in the reference's f32 order. With
+// FullScreenArgs, every candidate scored on the full surface.
+template <bool kFastDelta, class Args = ScreenArgs>
+__global__ void __launch_bounds__(kThreads, 3) screen_kernel(const __grid_constant__ Args A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Entry *E = reinterpret_cast<Entry *>(smem_raw);
     float *el = reinterpret_cast<float *>(E + A.sort_n);
@@ -132,7 +164,7 @@ __global__ void __launch_bounds__(kThreads, 3) screen_kernel(const __grid_consta
 #pragma unroll 1
         for (int r = 0; r < kRounds && valid && !has_def; ++r) {
             const CandHead h = cand_head(A.sc, seed_t, p);
-            const float s = synth_score<kFastDelta, false>(A.m, A.sc, el, seed_t, p, h, nullptr);
+            const float s = cand_score<kFastDelta>(A, el, seed_t, p, h);
             if (s >= ts) {
                 const unsigned long long k1 =
                     (static_cast<unsigned long long>(score_okey(s)) << 32) | static_cast<unsigned int>(~item);
@@ -375,8 +407,8 @@ __global__ void merge_kernel(const Entry *__restrict__ in, uint32_t nl, Entry *_
 
 // Survivor q of a final list: regenerate its genes and lineage from its
 // (item, candidate, draw) key and check the score bits against the key.
-template <bool kFastDelta>
-__device__ void regen_one(const DevModel &m, const SynthConst &sc, uint64_t seed, const float *el,
+template <bool kFastDelta, class Model>
+__device__ void regen_one(const Model &m, const SynthConst &sc, uint64_t seed, const float *el,
                           const Item *items, Ctrl *ctrl, const Entry *fin, uint32_t keep,
                           const unsigned long long *ids, const unsigned int *tribes, csx_survivor *out,
                           uint32_t q) {
@@ -395,7 +427,7 @@ __device__ void regen_one(const DevModel &m, const SynthConst &sc, uint64_t seed
     const uint64_t draw = it.draw0 + ddraw;
     const CandHead h = cand_head(sc, seed_t, draw);
     float genes[kNtot];
-    const float s = synth_score<kFastDelta, true>(m, sc, el, seed_t, draw, h, genes);
+    const float s = cand_genes<kFastDelta>(m, sc, el, seed_t, draw, h, genes);
     if (score_okey(s) != static_cast<unsigned int>(e.k1 >> 32)) atomicOr(&ctrl->err, kErrRegen);
     csx_survivor v;
     v.score = s;
@@ -418,6 +450,14 @@ __global__ void regen_kernel(const __grid_constant__ ScreenArgs A, const Entry *
                              unsigned long long *__restrict__ result) {
     (void)result;
     regen_one<kFastDelta>(A.m, A.sc, A.seed, A.el, A.items, A.ctrl, fin, A.keep, ids, tribes, out,
+                          blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+template <bool kFastDelta>
+__global__ void regen_full_kernel(const __grid_constant__ FullScreenArgs A, const Entry *__restrict__ fin,
+                                  const unsigned long long *__restrict__ ids,
+                                  const unsigned int *__restrict__ tribes, csx_survivor *__restrict__ out) {
+    regen_one<kFastDelta>(A.fm, A.sc, A.seed, A.el, A.items, A.ctrl, fin, A.keep, ids, tribes, out,
                           blockIdx.x * blockDim.x + threadIdx.x);
 }
 

@@ -53,6 +53,41 @@ class Model:
         return self._c
 
 
+class ModelFull:
+    """The full quadratic surface over all 29 genes (465 compact floats):
+    the quad-block extension docs/RESEARCH_V05C.md:99-102 queues, which the
+    reference's code does not have. Its score order is csx_screen.h's."""
+
+    NF = _lib.FULL_NF
+
+    def __init__(self, c: _lib.CsxModelFull):
+        self._c = c
+
+    @classmethod
+    def from_compact(cls, w) -> "ModelFull":
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        c = _lib.CsxModelFull()
+        check(lib().csx_model_full_from_compact(w.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                                int(w.shape[0]), ctypes.byref(c)), "full fromCompact")
+        return cls(c)
+
+    @property
+    def w0(self) -> float:
+        return float(self._c.w0)
+
+    @property
+    def w_lin(self) -> np.ndarray:
+        return np.ctypeslib.as_array(self._c.w_lin).copy()
+
+    @property
+    def w_quad(self) -> np.ndarray:
+        return np.ctypeslib.as_array(self._c.w_quad).copy()
+
+    @property
+    def c(self) -> _lib.CsxModelFull:
+        return self._c
+
+
 def parse_model_text(text: str) -> np.ndarray:
     """loadModel's text body, src/screen.zig:118-126: returns the compact weights."""
     b = text.encode()
@@ -101,14 +136,21 @@ def screen(cfg: Cfg, model: Model, elites, streams: Optional[Tuple[int, int]] = 
 
     streams=(a, b) screens only RNG streams a..b-1 of the generation (one
     rank's share when a generation is sharded by stream; merge the ranks'
-    survivors with parallel.merge_survivors)."""
+    survivors with parallel.merge_survivors). A ModelFull scores the
+    candidates on the full 29-gene quadratic surface instead."""
     e = _elites_array(elites)
     keep_n = min(int(cfg.keep), int(cfg.lambda_))
     out = np.zeros(max(keep_n, 1), dtype=SURVIVOR_DTYPE)
     n_out = ctypes.c_uint64(0)
     screened = ctypes.c_uint64(0)
     c = cfg.c()
-    if streams is None:
+    if isinstance(model, ModelFull):
+        if streams is not None:
+            raise ValueError("the full surface screens whole generations")
+        check(lib().csx_screen_full(ctypes.byref(c), ctypes.byref(model.c), e.ctypes.data, int(e.shape[0]),
+                                    out.ctypes.data, keep_n, ctypes.byref(n_out), ctypes.byref(screened)),
+              "screen_full")
+    elif streams is None:
         check(lib().csx_screen(ctypes.byref(c), ctypes.byref(model.c), e.ctypes.data, int(e.shape[0]),
                                out.ctypes.data, keep_n, ctypes.byref(n_out), ctypes.byref(screened)),
               "screen")
@@ -121,14 +163,16 @@ def screen(cfg: Cfg, model: Model, elites, streams: Optional[Tuple[int, int]] = 
 
 def score_genes(model: Model, genes):
     """Model.score (src/screen.zig:97-112) of the rows of a (n, >=29) float32
-    CUDA tensor, in the reference's f32 order, on the GPU."""
+    CUDA tensor, in the reference's f32 order, on the GPU (a ModelFull: the
+    full surface's score in its FMA order)."""
     import torch
 
     if not genes.is_cuda or genes.dtype != torch.float32 or genes.dim() != 2 or genes.stride(1) != 1:
         raise TypeError("genes must be a 2-D float32 CUDA tensor with contiguous rows")
     out = torch.empty(genes.shape[0], dtype=torch.float32, device=genes.device)
-    check(lib().csx_score(ctypes.byref(model.c), genes.data_ptr(), genes.shape[0], genes.stride(0), out.data_ptr(),
-                          torch.cuda.current_stream(genes.device).cuda_stream), "score")
+    fn = lib().csx_score_full if isinstance(model, ModelFull) else lib().csx_score
+    check(fn(ctypes.byref(model.c), genes.data_ptr(), genes.shape[0], genes.stride(0), out.data_ptr(),
+             torch.cuda.current_stream(genes.device).cuda_stream), "score")
     return out
 
 
@@ -170,9 +214,9 @@ def screen_device(cfg: Cfg, model: Model, elites_dev, out_dev, result_dev, strea
     if out_dev.numel() < keep_n * SURVIVOR_DTYPE.itemsize or result_dev.numel() < 4:
         raise ValueError("output buffers too small")
     c = cfg.c()
-    check(lib().csx_screen_device(ctypes.byref(c), ctypes.byref(model.c), elites_dev.data_ptr(), ne,
-                                  out_dev.data_ptr(), keep_n, result_dev.data_ptr(),
-                                  ctypes.c_void_p(stream.cuda_stream)), "screen_device")
+    fn = lib().csx_screen_full_device if isinstance(model, ModelFull) else lib().csx_screen_device
+    check(fn(ctypes.byref(c), ctypes.byref(model.c), elites_dev.data_ptr(), ne, out_dev.data_ptr(), keep_n,
+             result_dev.data_ptr(), ctypes.c_void_p(stream.cuda_stream)), "screen_device")
 
 
 def survivors_from_bytes(raw: np.ndarray, n: int) -> np.ndarray:
@@ -194,5 +238,5 @@ def limits() -> Tuple[int, int]:
     return int(k.value), int(e.value)
 
 
-__all__ = ["Model", "Cfg", "load_model", "parse_model_text", "screen", "run", "format_survivor",
+__all__ = ["Model", "ModelFull", "Cfg", "load_model", "parse_model_text", "screen", "run", "format_survivor",
            "screen_device", "survivors_from_bytes", "limits", "last_run_info", "VALID_N", "NTOT", "SURVIVOR_DTYPE"]

@@ -274,6 +274,40 @@ int csx_score(const csx_model *model, const float *d_genes, int64_t n, int ldg, 
 int csx_tc_score(const csx_model *model, int form, const float *d_genes, int64_t n, int ldg, float *d_out,
                  uint32_t *d_err, void *cuda_stream);
 
+/* ---- full quadratic surface -------------------------------------------------
+ * No counterpart in the reference's code: docs/RESEARCH_V05C.md:99-102 queues
+ * a surrogate whose quadratic block covers all 29 genes ("extend the quad
+ * block in v0.6"), since the six structural genes otherwise ride linear-only.
+ * Compact layout, CSX_FULL_NF = 465 floats: [0] constant, [1..29] linear
+ * terms, [30..465) g_i*g_j for j <= i < 29, i outer, j inner -- the v6
+ * layout's quadratic block extended from 16 to 29 genes (brain refits write
+ * it; see csx_surrogate.h). Its f32 score is defined by one FMA order:
+ *   r = w0; for k = 0..28: { t = w_lin[k]; for l = 0..k: t = fma(Q[k][l], g[l], t);
+ *                            r = fma(g[k], t, r); }
+ * i.e. w0 + sum_k g_k (w_k + sum_{l<=k} Q_kl g_l), the intercept counted
+ * once. Synthesis, streams, ties, survivors and counts are csx_screen's. */
+#define CSX_FULL_NF 465
+
+typedef struct csx_model_full {
+    float w0;
+    float w_lin[CSX_NTOT];
+    float w_quad[435]; /* (i, j <= i) at i*(i+1)/2 + j */
+} csx_model_full;
+
+/* n must be CSX_FULL_NF (else CSX_ERR_BAD_MODEL). */
+int csx_model_full_from_compact(const float *w, int n, csx_model_full *out);
+/* csx_screen / csx_screen_device with the candidates scored on the full
+ * surface. The precision-form flags are refused (CSX_ERR_BAD_ARGS). */
+int csx_screen_full(const csx_cfg *cfg, const csx_model_full *model, const csx_genome *elites, int n_elites,
+                    csx_survivor *out, uint64_t out_cap, uint64_t *n_out, uint64_t *screened);
+int csx_screen_full_device(const csx_cfg *cfg, const csx_model_full *model, const csx_genome *d_elites,
+                           int n_elites, csx_survivor *d_out, uint64_t out_cap, uint64_t *d_result,
+                           void *cuda_stream);
+/* The full surface's score of n genomes (rows of ldg >= 29 device floats) in
+ * the order above. Asynchronous on `cuda_stream`. */
+int csx_score_full(const csx_model_full *model, const float *d_genes, int64_t n, int ldg, float *d_out,
+                   void *cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -109,6 +109,38 @@ double orc_score_f64(const orc_model *m, const float *g) {
     return s;
 }
 
+/* ---- full quadratic surface (no reference code; see csx_oracle.h) ---------- */
+
+int orc_model_full_from_compact(const float *w, int n, orc_model_full *m) {
+    if (n != ORC_FULL_NF) return ORC_ERR_BAD_MODEL;
+    m->w0 = w[0];
+    for (int k = 0; k < ORC_NTOT; k++) m->w_lin[k] = w[1 + k];
+    for (int q = 0; q < ORC_FULL_NQ; q++) m->w_quad[q] = w[1 + ORC_NTOT + q];
+    return ORC_OK;
+}
+
+float orc_score_full(const orc_model_full *m, const float *g) {
+    float r = m->w0;
+    for (int k = 0; k < ORC_NTOT; k++) {
+        const float *q = &m->w_quad[k * (k + 1) / 2];
+        float t = m->w_lin[k];
+        for (int l = 0; l <= k; l++) t = fmaf(q[l], g[l], t);
+        r = fmaf(g[k], t, r);
+    }
+    return r;
+}
+
+double orc_score_full_f64(const orc_model_full *m, const float *g) {
+    double r = (double)m->w0;
+    for (int k = 0; k < ORC_NTOT; k++) {
+        const float *q = &m->w_quad[k * (k + 1) / 2];
+        double t = (double)m->w_lin[k];
+        for (int l = 0; l <= k; l++) t += (double)q[l] * (double)g[l];
+        r += (double)g[k] * t;
+    }
+    return r;
+}
+
 /* ---- text parsing (std.fmt.parseInt / parseFloat subset) ------------------- */
 
 /* Zig-style unsigned parse, base 10: optional '+', '-' only for zero,
@@ -297,6 +329,7 @@ typedef struct {
     const orc_model *m;
     const orc_genome *el;
     int ne;
+    const orc_model_full *mf; /* scores with the full surface when set */
 } orc_ctx;
 
 static float orc_synth(const orc_ctx *c, uint64_t *s, float *g, uint32_t *ea_i, uint32_t *eb_i) {
@@ -320,23 +353,35 @@ static float orc_synth(const orc_ctx *c, uint64_t *s, float *g, uint32_t *ea_i, 
         const uint64_t idx = (orc_splitmix_next(s) >> 32) % ORC_NTOT;
         g[idx] = orc_unit(s);
     }
-    return orc_score(c->m, g);
+    return c->mf ? orc_score_full(c->mf, g) : orc_score(c->m, g);
 }
 
-void orc_candidate(const orc_cfg *cfg, const orc_model *m, const orc_genome *el, int ne,
-                   uint64_t t, uint64_t draw, orc_survivor *out, uint64_t *next_draw) {
-    orc_ctx c = {cfg, m, el, ne};
-    const uint64_t seed_t = orc_stream_seed(cfg->seed, t);
+static void candidate_ctx(const orc_ctx *c, uint64_t t, uint64_t draw, orc_survivor *out,
+                          uint64_t *next_draw) {
+    const orc_genome *el = c->el;
+    const uint64_t seed_t = orc_stream_seed(c->cfg->seed, t);
     uint64_t s = seed_t + draw * GOLDEN;
     uint32_t a, b;
     memset(out, 0, sizeof(*out));
-    out->score = orc_synth(&c, &s, out->g, &a, &b);
+    out->score = orc_synth(c, &s, out->g, &a, &b);
     out->pa = el[a].id;
     out->pb = el[b].id;
     out->tribe = el[a].tribe;
     out->stream = t;
     out->draw = draw;
     if (next_draw) *next_draw = (s - seed_t) * 0xF1DE83E19937733Dull; /* s = seed + d*G, G^-1 */
+}
+
+void orc_candidate(const orc_cfg *cfg, const orc_model *m, const orc_genome *el, int ne,
+                   uint64_t t, uint64_t draw, orc_survivor *out, uint64_t *next_draw) {
+    const orc_ctx c = {cfg, m, el, ne, NULL};
+    candidate_ctx(&c, t, draw, out, next_draw);
+}
+
+void orc_candidate_full(const orc_cfg *cfg, const orc_model_full *m, const orc_genome *el, int ne,
+                        uint64_t t, uint64_t draw, orc_survivor *out, uint64_t *next_draw) {
+    const orc_ctx c = {cfg, NULL, el, ne, m};
+    candidate_ctx(&c, t, draw, out, next_draw);
 }
 
 int orc_stream_dump(const orc_cfg *cfg, const orc_model *m, const orc_genome *el, int ne,
@@ -524,9 +569,10 @@ static void *orc_worker(void *arg) {
     return NULL;
 }
 
-int orc_screen(const orc_cfg *cfg, const orc_model *m, const orc_genome *el, int ne,
-               int cpu_threads, orc_survivor *out, uint64_t out_cap, uint64_t *n_out,
-               uint64_t *screened) {
+static int screen_ctx(const orc_ctx *ctx, int cpu_threads, orc_survivor *out, uint64_t out_cap,
+                      uint64_t *n_out, uint64_t *screened) {
+    const orc_cfg *cfg = ctx->cfg;
+    const int ne = ctx->ne;
     *n_out = 0;
     if (screened) *screened = 0;
     if (ne < 2) return ORC_ERR_NEED_TWO_ELITES;
@@ -535,10 +581,7 @@ int orc_screen(const orc_cfg *cfg, const orc_model *m, const orc_genome *el, int
     if (T < 1) T = 1;
     orc_run r;
     memset(&r, 0, sizeof(r));
-    r.c.cfg = cfg;
-    r.c.m = m;
-    r.c.el = el;
-    r.c.ne = ne;
+    r.c = *ctx;
     r.T = T;
     r.per = cfg->lambda / T;
     r.keep = cfg->keep;
@@ -592,7 +635,7 @@ int orc_screen(const orc_cfg *cfg, const orc_model *m, const orc_genome *el, int
         if (cfg->flags & ORC_FLAG_AS_SHIPPED) outn = 0;
         if (outn > out_cap) outn = out_cap;
         for (uint64_t q = 0; q < outn; q++) {
-            orc_candidate(cfg, m, el, ne, all[q].stream, all[q].draw, &out[q], NULL);
+            candidate_ctx(ctx, all[q].stream, all[q].draw, &out[q], NULL);
             out[q].index = all[q].index;
         }
         *n_out = outn;
@@ -607,4 +650,18 @@ done:
     free(args);
     pthread_mutex_destroy(&r.mu);
     return rc;
+}
+
+int orc_screen(const orc_cfg *cfg, const orc_model *m, const orc_genome *el, int ne,
+               int cpu_threads, orc_survivor *out, uint64_t out_cap, uint64_t *n_out,
+               uint64_t *screened) {
+    const orc_ctx c = {cfg, m, el, ne, NULL};
+    return screen_ctx(&c, cpu_threads, out, out_cap, n_out, screened);
+}
+
+int orc_screen_full(const orc_cfg *cfg, const orc_model_full *m, const orc_genome *el, int ne,
+                    int cpu_threads, orc_survivor *out, uint64_t out_cap, uint64_t *n_out,
+                    uint64_t *screened) {
+    const orc_ctx c = {cfg, NULL, el, ne, m};
+    return screen_ctx(&c, cpu_threads, out, out_cap, n_out, screened);
 }

@@ -124,6 +124,35 @@ int orc_screen(const orc_cfg *cfg, const orc_model *m, const orc_genome *el, int
                int cpu_threads, orc_survivor *out, uint64_t out_cap, uint64_t *n_out,
                uint64_t *screened);
 
+/* ---- full quadratic surface ----------------------------------------------
+ * No reference code: docs/RESEARCH_V05C.md:99-102 queues a surrogate whose
+ * quadratic block covers all 29 genes ("extend the quad block in v0.6").
+ * Compact layout (ORC_FULL_NF = 465 floats): [0] constant, [1..29] linear
+ * terms, then g_i*g_j for j <= i < 29, i outer, j inner -- the v6 layout's
+ * quadratic block extended from 16 to 29 genes. The f32 score is defined by
+ * this FMA order (one rounding per fmaf):
+ *   r = w0; for k in 0..28: t = w_lin[k]; for l in 0..k: t = fmaf(Q[k][l], g[l], t);
+ *                           r = fmaf(g[k], t, r)
+ * i.e. w0 + sum_k g_k (w_k + sum_{l<=k} Q_kl g_l), the intercept counted once. */
+#define ORC_FULL_NF 465
+#define ORC_FULL_NQ 435
+
+typedef struct orc_model_full {
+    float w0;
+    float w_lin[ORC_NTOT];
+    float w_quad[ORC_FULL_NQ]; /* (i, j <= i) at i*(i+1)/2 + j */
+} orc_model_full;
+
+int orc_model_full_from_compact(const float *w, int n, orc_model_full *m);
+float orc_score_full(const orc_model_full *m, const float *g);
+double orc_score_full_f64(const orc_model_full *m, const float *g);
+/* orc_candidate / orc_screen with the full surface scoring the candidates. */
+void orc_candidate_full(const orc_cfg *cfg, const orc_model_full *m, const orc_genome *el, int ne,
+                        uint64_t t, uint64_t draw, orc_survivor *out, uint64_t *next_draw);
+int orc_screen_full(const orc_cfg *cfg, const orc_model_full *m, const orc_genome *el, int ne,
+                    int cpu_threads, orc_survivor *out, uint64_t out_cap, uint64_t *n_out,
+                    uint64_t *screened);
+
 /* Candidate-start walk: number of candidates of stream t that start before
  * draw position `end`, starting from the candidate at draw `start`. */
 uint64_t orc_walk(const orc_cfg *cfg, uint64_t t, uint64_t start, uint64_t end,

@@ -38,6 +38,14 @@ class OrcModel(ctypes.Structure):
                 ("w_quad", ctypes.c_float * 256)]
 
 
+FULL_NF = 465  # compact length of the full quadratic surface (csx_oracle.h)
+
+
+class OrcModelFull(ctypes.Structure):
+    _fields_ = [("w0", ctypes.c_float), ("w_lin", ctypes.c_float * NTOT),
+                ("w_quad", ctypes.c_float * 435)]
+
+
 class OrcCfg(ctypes.Structure):
     _fields_ = [("lambda_", ctypes.c_uint64), ("keep", ctypes.c_uint64), ("seed", ctypes.c_uint64),
                 ("threads", ctypes.c_uint64), ("sigma", ctypes.c_float), ("jump_p", ctypes.c_float),
@@ -75,6 +83,18 @@ def lib():
         l.orc_screen.argtypes = [ctypes.POINTER(OrcCfg), ctypes.POINTER(OrcModel), ctypes.c_void_p,
                                  ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64,
                                  ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
+        l.orc_model_full_from_compact.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.c_int,
+                                                  ctypes.POINTER(OrcModelFull)]
+        l.orc_score_full.restype = ctypes.c_float
+        l.orc_score_full.argtypes = [ctypes.POINTER(OrcModelFull), ctypes.c_void_p]
+        l.orc_score_full_f64.restype = ctypes.c_double
+        l.orc_score_full_f64.argtypes = [ctypes.POINTER(OrcModelFull), ctypes.c_void_p]
+        l.orc_candidate_full.argtypes = [ctypes.POINTER(OrcCfg), ctypes.POINTER(OrcModelFull), ctypes.c_void_p,
+                                         ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p,
+                                         ctypes.POINTER(ctypes.c_uint64)]
+        l.orc_screen_full.argtypes = [ctypes.POINTER(OrcCfg), ctypes.POINTER(OrcModelFull), ctypes.c_void_p,
+                                      ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64,
+                                      ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
         l.orc_walk.restype = ctypes.c_uint64
         l.orc_walk.argtypes = [ctypes.POINTER(OrcCfg), ctypes.c_uint64, ctypes.c_uint64,
                                ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]
@@ -97,6 +117,21 @@ def model_from_compact(w):
     return m
 
 
+def model_full_from_compact(w):
+    """The full quadratic surface (465 compact floats; csx_oracle.h)."""
+    w = np.ascontiguousarray(w, dtype=np.float32)
+    m = OrcModelFull()
+    rc = lib().orc_model_full_from_compact(w.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), len(w),
+                                           ctypes.byref(m))
+    if rc:
+        raise ValueError(f"orc_model_full_from_compact: {rc}")
+    return m
+
+
+def _full(m) -> bool:
+    return isinstance(m, OrcModelFull)
+
+
 def model_parse(text: str) -> np.ndarray:
     b = text.encode()
     w = (ctypes.c_float * 166)()
@@ -109,12 +144,14 @@ def model_parse(text: str) -> np.ndarray:
 
 def score(m, g) -> np.float32:
     g = np.ascontiguousarray(g, dtype=np.float32)
-    return np.float32(lib().orc_score(ctypes.byref(m), g.ctypes.data))
+    f = lib().orc_score_full if _full(m) else lib().orc_score
+    return np.float32(f(ctypes.byref(m), g.ctypes.data))
 
 
 def score_f64(m, g) -> float:
     g = np.ascontiguousarray(g, dtype=np.float32)
-    return float(lib().orc_score_f64(ctypes.byref(m), g.ctypes.data))
+    f = lib().orc_score_full_f64 if _full(m) else lib().orc_score_f64
+    return float(f(ctypes.byref(m), g.ctypes.data))
 
 
 def parse_line(line: str, flags: int = 0):
@@ -146,8 +183,8 @@ def candidate(c: OrcCfg, m, elites, t: int, draw: int):
     e = np.ascontiguousarray(elites, dtype=GENOME_DTYPE)
     out = np.zeros(1, dtype=SURVIVOR_DTYPE)
     nxt = ctypes.c_uint64(0)
-    lib().orc_candidate(ctypes.byref(c), ctypes.byref(m), e.ctypes.data, len(e), t, draw,
-                        out.ctypes.data, ctypes.byref(nxt))
+    f = lib().orc_candidate_full if _full(m) else lib().orc_candidate
+    f(ctypes.byref(c), ctypes.byref(m), e.ctypes.data, len(e), t, draw, out.ctypes.data, ctypes.byref(nxt))
     return out[0], int(nxt.value)
 
 
@@ -158,8 +195,9 @@ def screen(c: OrcCfg, m, elites, cpu_threads: int = 0):
     out = np.zeros(max(1, cap), dtype=SURVIVOR_DTYPE)
     n = ctypes.c_uint64(0)
     scr = ctypes.c_uint64(0)
-    rc = lib().orc_screen(ctypes.byref(c), ctypes.byref(m), e.ctypes.data, len(e), int(cpu_threads),
-                          out.ctypes.data, cap, ctypes.byref(n), ctypes.byref(scr))
+    f = lib().orc_screen_full if _full(m) else lib().orc_screen
+    rc = f(ctypes.byref(c), ctypes.byref(m), e.ctypes.data, len(e), int(cpu_threads),
+           out.ctypes.data, cap, ctypes.byref(n), ctypes.byref(scr))
     if rc:
         raise ValueError(f"orc_screen: {rc}")
     return out[: n.value], int(scr.value)
