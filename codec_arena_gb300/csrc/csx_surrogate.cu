@@ -21,28 +21,36 @@
 
 namespace {
 
-constexpr int kQuadGenes = 16;
+constexpr int kQuadGenes = 16;                             // the reference layouts' quadratic block
 constexpr int kNQuad = kQuadGenes * (kQuadGenes + 1) / 2;  // 136
 constexpr int kMaxLin = 29;
 constexpr int kMinFeat = 1 + kQuadGenes + kNQuad;  // 153
 constexpr int kMaxFeat = 1 + kMaxLin + kNQuad;     // 166
+// The full surface (csx_screen.h): the quadratic block over all 29 genes.
+constexpr int kNQuadFull = kMaxLin * (kMaxLin + 1) / 2;  // 435
+constexpr int kFullFeat = 1 + kMaxLin + kNQuadFull;      // 465
+constexpr int kFeatCap = kFullFeat;                      // stride of per-feature partial sums
 constexpr int kRowThreads = 256;                   // rows per tile in the row kernels
 constexpr int kPartBlocks = 152;                   // fixed: the reductions' summation order never changes
+constexpr int kPartBlocksFull = 64;                // the same for the full layout's normal equations
 constexpr int kGramRows = 32;                      // rows per Φ tile in the normal equations
 constexpr int kGramBlk = 4;                        // each thread owns a 4×4 block of ΦᵀΦ
-constexpr int kGramNb = (kMaxFeat + kGramBlk - 1) / kGramBlk;  // 42 block rows at most
-constexpr int kGramPairs = kGramNb * (kGramNb + 1) / 2;        // 903 lower-triangle blocks at most
-constexpr int kGramFeatPad = kGramNb * kGramBlk;               // 168
+constexpr int kGramThreads = 1024;                 // 4×4 blocks per CTA (CTAs along y split the blocks)
 constexpr int kSolveThreads = 1024;
 
 __host__ __device__ constexpr int tri(int i) { return i * (i + 1) / 2; }
+__host__ __device__ constexpr int gram_nb(int nf) { return (nf + kGramBlk - 1) / kGramBlk; }
+__host__ __device__ constexpr int gram_pairs(int nf) { return tri(gram_nb(nf)); }
+constexpr int kGramFeatPadFull = gram_nb(kFullFeat) * kGramBlk;  // 468
 
 // Coefficients as the row kernels read them: linear terms padded with zeros to
-// 29, quadratic terms packed (i, j <= i).
-struct CoefF {
+// 29, quadratic terms packed (i, j <= i) over the first QG genes (16: the
+// reference's layouts; 29: the full surface).
+template <int QG>
+struct CoefT {
     float c0;
     float lin[kMaxLin];
-    float q[kNQuad];
+    float q[QG * (QG + 1) / 2];
 };
 
 template <int P>
@@ -51,9 +59,10 @@ __device__ __forceinline__ float in_prec(float x) {
     return x;
 }
 
-template <int P>
-__device__ void load_coef(CoefF &s, const float *coef, int ng) {
-    for (int i = threadIdx.x; i < 1 + kMaxLin + kNQuad; i += blockDim.x) {
+template <int P, int QG>
+__device__ void load_coef(CoefT<QG> &s, const float *coef, int ng) {
+    constexpr int nq = QG * (QG + 1) / 2;
+    for (int i = threadIdx.x; i < 1 + kMaxLin + nq; i += blockDim.x) {
         float v;
         if (i == 0) {
             v = coef[0];
@@ -83,26 +92,42 @@ __device__ __forceinline__ void read_row(float (&g)[kMaxLin], const float *tile,
     for (int k = 0; k < kMaxLin; ++k) g[k] = (k < ng) ? in_prec<P>(tile[threadIdx.x * st + k]) : 0.0f;
 }
 
-__device__ __forceinline__ float score_f32(const CoefF &c, const float (&g)[kMaxLin]) {
-    float s = c.c0;
+// FP32 score. The reference layouts: linear terms, then the quadratic rows.
+// The full surface: csx_screen.h's defined FMA order (the screen's score).
+template <int QG>
+__device__ __forceinline__ float score_f32(const CoefT<QG> &c, const float (&g)[kMaxLin]) {
+    if constexpr (QG == kMaxLin) {
+        float r = c.c0;
 #pragma unroll
-    for (int k = 0; k < kMaxLin; ++k) s = __fmaf_rn(c.lin[k], g[k], s);
+        for (int k = 0; k < kMaxLin; ++k) {
+            float t = c.lin[k];
 #pragma unroll
-    for (int i = 0; i < kQuadGenes; ++i) {
-        float t = 0.0f;
+            for (int l = 0; l <= k; ++l) t = __fmaf_rn(c.q[tri(k) + l], g[l], t);
+            r = __fmaf_rn(g[k], t, r);
+        }
+        return r;
+    } else {
+        float s = c.c0;
 #pragma unroll
-        for (int j = 0; j <= i; ++j) t = __fmaf_rn(c.q[tri(i) + j], g[j], t);
-        s = __fmaf_rn(t, g[i], s);
+        for (int k = 0; k < kMaxLin; ++k) s = __fmaf_rn(c.lin[k], g[k], s);
+#pragma unroll
+        for (int i = 0; i < QG; ++i) {
+            float t = 0.0f;
+#pragma unroll
+            for (int j = 0; j <= i; ++j) t = __fmaf_rn(c.q[tri(i) + j], g[j], t);
+            s = __fmaf_rn(t, g[i], s);
+        }
+        return s;
     }
-    return s;
 }
 
-// ∂score/∂g_k = lin_k + Σ_{j<=k} q_kj g_j + Σ_{i>=k} q_ik g_i (k < 16).
-__device__ __forceinline__ void grad_f32(const CoefF &c, const float (&g)[kMaxLin], float (&d)[kMaxLin]) {
+// ∂score/∂g_k = lin_k + Σ_{j<=k} q_kj g_j + Σ_{i>=k} q_ik g_i (k < QG).
+template <int QG>
+__device__ __forceinline__ void grad_f32(const CoefT<QG> &c, const float (&g)[kMaxLin], float (&d)[kMaxLin]) {
 #pragma unroll
     for (int k = 0; k < kMaxLin; ++k) d[k] = c.lin[k];
 #pragma unroll
-    for (int i = 0; i < kQuadGenes; ++i) {
+    for (int i = 0; i < QG; ++i) {
 #pragma unroll
         for (int j = 0; j <= i; ++j) {
             const float q = c.q[tri(i) + j];
@@ -114,14 +139,14 @@ __device__ __forceinline__ void grad_f32(const CoefF &c, const float (&g)[kMaxLi
 
 __host__ __device__ inline int stride_for(int ng) { return ((ng + 1) & 1) ? ng + 1 : ng + 2; }  // odd, >= ng + 1
 
-template <int P>
+template <int P, int QG>
 __global__ void __launch_bounds__(kRowThreads) sg_forward_kernel(const float *__restrict__ coef, int ng,
                                                                  const float *__restrict__ genes, int64_t n,
                                                                  int ldg, float *__restrict__ score) {
-    __shared__ CoefF c;
+    __shared__ CoefT<QG> c;
     extern __shared__ float tile[];
     const int st = stride_for(ng);
-    load_coef<P>(c, coef, ng);
+    load_coef<P, QG>(c, coef, ng);
     for (int64_t r0 = static_cast<int64_t>(blockIdx.x) * kRowThreads; r0 < n;
          r0 += static_cast<int64_t>(gridDim.x) * kRowThreads) {
         __syncthreads();
@@ -135,13 +160,15 @@ __global__ void __launch_bounds__(kRowThreads) sg_forward_kernel(const float *__
     }
 }
 
+template <int QG>
 __global__ void __launch_bounds__(kRowThreads) sg_forward_f64_kernel(const double *__restrict__ coef, int ng,
                                                                      const float *__restrict__ genes, int64_t n,
                                                                      int ldg, double *__restrict__ score) {
-    __shared__ double lin[kMaxLin], q[kNQuad], c0;
+    constexpr int nq = QG * (QG + 1) / 2;
+    __shared__ double lin[kMaxLin], q[nq], c0;
     extern __shared__ float tile[];
     const int st = stride_for(ng);
-    for (int i = threadIdx.x; i < 1 + kMaxLin + kNQuad; i += blockDim.x) {
+    for (int i = threadIdx.x; i < 1 + kMaxLin + nq; i += blockDim.x) {
         if (i == 0) c0 = coef[0];
         else if (i <= kMaxLin) lin[i - 1] = (i <= ng) ? coef[i] : 0.0;
         else q[i - 1 - kMaxLin] = coef[1 + ng + (i - 1 - kMaxLin)];
@@ -159,7 +186,7 @@ __global__ void __launch_bounds__(kRowThreads) sg_forward_f64_kernel(const doubl
 #pragma unroll
             for (int k = 0; k < kMaxLin; ++k) s = fma(lin[k], g[k], s);
 #pragma unroll
-            for (int i = 0; i < kQuadGenes; ++i) {
+            for (int i = 0; i < QG; ++i) {
                 double t = 0.0;
 #pragma unroll
                 for (int j = 0; j <= i; ++j) t = fma(q[tri(i) + j], g[j], t);
@@ -170,15 +197,15 @@ __global__ void __launch_bounds__(kRowThreads) sg_forward_f64_kernel(const doubl
     }
 }
 
-template <int P>
+template <int P, int QG>
 __global__ void __launch_bounds__(kRowThreads) sg_grad_genes_kernel(const float *__restrict__ coef, int ng,
                                                                     const float *__restrict__ genes, int64_t n,
                                                                     int ldg, const float *__restrict__ gout,
                                                                     float *__restrict__ dgenes) {
-    __shared__ CoefF c;
+    __shared__ CoefT<QG> c;
     extern __shared__ float tile[];
     const int st = stride_for(ng);
-    load_coef<P>(c, coef, ng);
+    load_coef<P, QG>(c, coef, ng);
     for (int64_t r0 = static_cast<int64_t>(blockIdx.x) * kRowThreads; r0 < n;
          r0 += static_cast<int64_t>(gridDim.x) * kRowThreads) {
         __syncthreads();
@@ -232,12 +259,18 @@ template <typename TG>
 __global__ void __launch_bounds__(kRowThreads) sg_grad_coef_kernel(int ng, int nf, const float *__restrict__ genes,
                                                                    int64_t n, int ldg, const TG *__restrict__ gout,
                                                                    double *__restrict__ part) {
+    constexpr int kPer = (kFeatCap + kRowThreads - 1) / kRowThreads;  // features per thread (2)
     extern __shared__ float tile[];
     __shared__ double go_s[kRowThreads];
     const int st = stride_for(ng);
-    int a = 0, b = 0;
-    if (threadIdx.x < nf) feature_pair(threadIdx.x, ng, a, b);
-    double acc = 0.0;
+    int a[kPer], b[kPer];
+#pragma unroll
+    for (int m = 0; m < kPer; ++m) {
+        a[m] = b[m] = 0;
+        const int f = threadIdx.x + m * kRowThreads;
+        if (f < nf) feature_pair(f, ng, a[m], b[m]);
+    }
+    double acc[kPer] = {};
     for (int64_t r0 = static_cast<int64_t>(blockIdx.x) * kRowThreads; r0 < n;
          r0 += static_cast<int64_t>(gridDim.x) * kRowThreads) {
         __syncthreads();
@@ -248,14 +281,22 @@ __global__ void __launch_bounds__(kRowThreads) sg_grad_coef_kernel(int ng, int n
             go_s[threadIdx.x] = static_cast<double>(gout[r0 + threadIdx.x]);
         }
         __syncthreads();
-        if (threadIdx.x < nf) {
-            for (int r = 0; r < rows; ++r) {
-                const double phi = static_cast<double>(tile[r * st + a]) * static_cast<double>(tile[r * st + b]);
-                acc = fma(go_s[r], phi, acc);
+#pragma unroll
+        for (int m = 0; m < kPer; ++m) {
+            if (threadIdx.x + m * kRowThreads < nf) {
+                for (int r = 0; r < rows; ++r) {
+                    const double phi =
+                        static_cast<double>(tile[r * st + a[m]]) * static_cast<double>(tile[r * st + b[m]]);
+                    acc[m] = fma(go_s[r], phi, acc[m]);
+                }
             }
         }
     }
-    if (threadIdx.x < nf) part[static_cast<int64_t>(blockIdx.x) * kMaxFeat + threadIdx.x] = acc;
+#pragma unroll
+    for (int m = 0; m < kPer; ++m) {
+        const int f = threadIdx.x + m * kRowThreads;
+        if (f < nf) part[static_cast<int64_t>(blockIdx.x) * kFeatCap + f] = acc[m];
+    }
 }
 
 __global__ void sg_sum_parts_kernel(const double *__restrict__ part, int nparts, int stride, int nf,
@@ -267,24 +308,34 @@ __global__ void sg_sum_parts_kernel(const double *__restrict__ part, int nparts,
     out[f] = s;
 }
 
-// Normal equations: thread t owns the 4×4 block (bi, bj), bj <= bi, of ΦᵀΦ;
-// threads t < nf also accumulate (Φᵀy)_t. Φ for kGramRows rows is staged in
-// shared memory in FP64 (exact: a product of two f32 genes).
-__global__ void __launch_bounds__(1024) sg_gram_kernel(int ng, int nf, const float *__restrict__ genes, int64_t n,
-                                                       int ldg, const double *__restrict__ fit,
-                                                       double *__restrict__ part_g, double *__restrict__ part_r) {
-    extern __shared__ double phi[];  // [kGramRows][kGramFeatPad]
+// Normal equations: thread t of CTA column y owns the 4×4 block number
+// y·1024 + t, (bi, bj) with bj <= bi, of ΦᵀΦ; CTA row x accumulates rows of
+// its chunk. Column 0's threads t < nf also accumulate (Φᵀy)_t. Φ for
+// kGramRows rows is staged in shared memory in FP64 (exact: a product of two
+// f32 genes), featpad = 4·ceil(nf/4) features per row.
+__global__ void __launch_bounds__(kGramThreads) sg_gram_kernel(int ng, int nf, const float *__restrict__ genes,
+                                                               int64_t n, int ldg, const double *__restrict__ fit,
+                                                               double *__restrict__ part_g,
+                                                               double *__restrict__ part_r) {
+    extern __shared__ double phi[];  // [kGramRows][featpad]
     __shared__ float gs[kGramRows][kMaxLin + 1];
     __shared__ double ys[kGramRows];
-    const int nb = (nf + kGramBlk - 1) / kGramBlk;
-    const int npairs = nb * (nb + 1) / 2;
+    __shared__ unsigned char fa[kGramFeatPadFull], fb[kGramFeatPadFull];  // feature f = x[fa]·x[fb]
+    const int nb = gram_nb(nf), featpad = nb * kGramBlk;
+    const int npairs = tri(nb);
     const int t = threadIdx.x;
+    for (int f = t; f < nf; f += blockDim.x) {
+        int a, b;
+        feature_pair(f, ng, a, b);
+        fa[f] = static_cast<unsigned char>(a);
+        fb[f] = static_cast<unsigned char>(b);
+    }
+    const int pt = blockIdx.y * kGramThreads + t;  // this thread's block number
     int bi = 0;
-    while (tri(bi + 1) <= t) ++bi;
-    const int bj = t - tri(bi);
-    const bool owner = t < npairs;
-    int fa = 0, fb = 0;
-    if (t < nf) feature_pair(t, ng, fa, fb);
+    while (tri(bi + 1) <= pt) ++bi;
+    const int bj = pt - tri(bi);
+    const bool owner = pt < npairs;
+    const bool rhs_here = blockIdx.y == 0 && t < nf && fit;
     double acc[kGramBlk][kGramBlk] = {};
     double racc = 0.0;
     const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
@@ -302,20 +353,16 @@ __global__ void __launch_bounds__(1024) sg_gram_kernel(int ng, int nf, const flo
             ys[t] = fit ? fit[r0 + t] : 0.0;
         }
         __syncthreads();
-        for (int idx = t; idx < kGramRows * kGramFeatPad; idx += blockDim.x) {
-            const int r = idx / kGramFeatPad, f = idx - r * kGramFeatPad;
+        for (int idx = t; idx < kGramRows * featpad; idx += blockDim.x) {
+            const int r = idx / featpad, f = idx - r * featpad;
             double v = 0.0;
-            if (r < rows && f < nf) {
-                int a, b;
-                feature_pair(f, ng, a, b);
-                v = static_cast<double>(gs[r][a]) * static_cast<double>(gs[r][b]);
-            }
+            if (r < rows && f < nf) v = static_cast<double>(gs[r][fa[f]]) * static_cast<double>(gs[r][fb[f]]);
             phi[idx] = v;
         }
         __syncthreads();
         if (owner) {
             for (int r = 0; r < rows; ++r) {
-                const double *pr = phi + r * kGramFeatPad;
+                const double *pr = phi + r * featpad;
                 double xa[kGramBlk], xb[kGramBlk];
 #pragma unroll
                 for (int u = 0; u < kGramBlk; ++u) {
@@ -328,26 +375,25 @@ __global__ void __launch_bounds__(1024) sg_gram_kernel(int ng, int nf, const flo
                     for (int v = 0; v < kGramBlk; ++v) acc[u][v] = fma(xa[u], xb[v], acc[u][v]);
             }
         }
-        if (t < nf && fit) {
-            for (int r = 0; r < rows; ++r) racc = fma(ys[r], phi[r * kGramFeatPad + t], racc);
+        if (rhs_here) {
+            for (int r = 0; r < rows; ++r) racc = fma(ys[r], phi[r * featpad + t], racc);
         }
     }
     if (owner) {
-        double *dst = part_g + (static_cast<int64_t>(blockIdx.x) * kGramPairs + t) * (kGramBlk * kGramBlk);
+        double *dst = part_g + (static_cast<int64_t>(blockIdx.x) * npairs + pt) * (kGramBlk * kGramBlk);
 #pragma unroll
         for (int u = 0; u < kGramBlk; ++u)
 #pragma unroll
             for (int v = 0; v < kGramBlk; ++v) dst[u * kGramBlk + v] = acc[u][v];
     }
-    if (t < nf) part_r[static_cast<int64_t>(blockIdx.x) * kMaxFeat + t] = racc;
+    if (rhs_here) part_r[static_cast<int64_t>(blockIdx.x) * kFeatCap + t] = racc;
 }
 
 __global__ void sg_gram_sum_kernel(const double *__restrict__ part_g, int nparts, int nf, double *__restrict__ gram) {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;  // (pair, u, v)
-    const int nb = (nf + kGramBlk - 1) / kGramBlk;
-    const int npairs = nb * (nb + 1) / 2;
-    if (e >= npairs * kGramBlk * kGramBlk) return;
-    const int t = e / (kGramBlk * kGramBlk), uv = e - t * (kGramBlk * kGramBlk);
+    const int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;  // (pair, u, v)
+    const int npairs = gram_pairs(nf);
+    if (e >= static_cast<int64_t>(npairs) * kGramBlk * kGramBlk) return;
+    const int t = static_cast<int>(e / (kGramBlk * kGramBlk)), uv = static_cast<int>(e % (kGramBlk * kGramBlk));
     const int u = uv / kGramBlk, v = uv - u * kGramBlk;
     int bi = 0;
     while (tri(bi + 1) <= t) ++bi;
@@ -355,18 +401,17 @@ __global__ void sg_gram_sum_kernel(const double *__restrict__ part_g, int nparts
     const int a = bi * kGramBlk + u, b = bj * kGramBlk + v;
     if (a >= nf || b >= nf) return;
     double s = 0.0;
-    for (int p = 0; p < nparts; ++p) s += part_g[(static_cast<int64_t>(p) * kGramPairs + t) * (kGramBlk * kGramBlk) + uv];
+    for (int p = 0; p < nparts; ++p) s += part_g[(static_cast<int64_t>(p) * npairs + t) * (kGramBlk * kGramBlk) + uv];
     gram[static_cast<int64_t>(a) * nf + b] = s;
     gram[static_cast<int64_t>(b) * nf + a] = s;
 }
 
-// (G + αI) w = rhs + α·prior by Cholesky, FP64, packed lower triangle in
-// shared memory, one CTA of 32×32 threads.
-__global__ void __launch_bounds__(kSolveThreads) sg_ridge_solve_kernel(int n, const double *__restrict__ gram,
-                                                                       const double *__restrict__ rhs, double alpha,
-                                                                       const double *__restrict__ prior,
-                                                                       double *__restrict__ w, int *status) {
-    extern __shared__ double L[];  // tri(n) entries, then y[n]
+// (G + αI) w = rhs + α·prior by Cholesky, FP64, packed lower triangle L
+// (tri(n) entries, then y[n]) in shared memory up to 166 coefficients, in a
+// global scratch for the full surface's 465; one CTA of 32×32 threads.
+__device__ void ridge_solve_body(double *L, int n, const double *__restrict__ gram, const double *__restrict__ rhs,
+                                 double alpha, const double *__restrict__ prior, double *__restrict__ w,
+                                 int *status) {
     double *y = L + tri(n);
     __shared__ int bad;
     const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
@@ -409,13 +454,31 @@ __global__ void __launch_bounds__(kSolveThreads) sg_ridge_solve_kernel(int n, co
     if (tid == 0) *status = bad;
 }
 
+__global__ void __launch_bounds__(kSolveThreads) sg_ridge_solve_kernel(int n, const double *__restrict__ gram,
+                                                                       const double *__restrict__ rhs, double alpha,
+                                                                       const double *__restrict__ prior,
+                                                                       double *__restrict__ w, int *status) {
+    extern __shared__ double L[];
+    ridge_solve_body(L, n, gram, rhs, alpha, prior, w, status);
+}
+
+__global__ void __launch_bounds__(kSolveThreads) sg_ridge_solve_global_kernel(int n, const double *__restrict__ gram,
+                                                                              const double *__restrict__ rhs,
+                                                                              double alpha,
+                                                                              const double *__restrict__ prior,
+                                                                              double *__restrict__ w, int *status,
+                                                                              double *scratch) {
+    ridge_solve_body(scratch, n, gram, rhs, alpha, prior, w, status);
+}
+
+template <int QG>
 __global__ void __launch_bounds__(kRowThreads) sg_ascend_kernel(const float *__restrict__ coef, int ng,
                                                                 float *__restrict__ genes, int64_t n, int ldg,
                                                                 float eta, int steps, float *__restrict__ score) {
-    __shared__ CoefF c;
+    __shared__ CoefT<QG> c;
     extern __shared__ float tile[];
     const int st = stride_for(ng);
-    load_coef<CSX_SG_FP32>(c, coef, ng);
+    load_coef<CSX_SG_FP32, QG>(c, coef, ng);
     for (int64_t r0 = static_cast<int64_t>(blockIdx.x) * kRowThreads; r0 < n;
          r0 += static_cast<int64_t>(gridDim.x) * kRowThreads) {
         __syncthreads();
@@ -426,6 +489,9 @@ __global__ void __launch_bounds__(kRowThreads) sg_ascend_kernel(const float *__r
             float g[kMaxLin], d[kMaxLin];
             read_row<CSX_SG_FP32>(g, tile, st, ng);
             for (int s = 0; s < steps; ++s) {
+                // keep the coefficient loads inside the loop: hoisted, the full
+                // surface's 435 quadratic terms would not fit in registers
+                asm volatile("" ::: "memory");
                 grad_f32(c, g, d);
 #pragma unroll
                 for (int k = 0; k < kMaxLin; ++k)
@@ -455,12 +521,21 @@ __global__ void __launch_bounds__(kRowThreads) sg_ascend_kernel(const float *__r
         }                                                                                   \
     } while (0)
 
+// nf -> genes: the reference layouts (153..166: 16-gene quadratic block, ng
+// genes linear) or the full surface (465: 29 genes, all quadratic).
 int check_layout(int nf, int ldg, int64_t n, int &ng) {
-    if (nf < kMinFeat || nf > kMaxFeat || n < 0) return CSX_ERR_BAD_ARGS;
-    ng = nf - 1 - kNQuad;
+    if (n < 0) return CSX_ERR_BAD_ARGS;
+    if (nf == kFullFeat) {
+        ng = kMaxLin;
+    } else {
+        if (nf < kMinFeat || nf > kMaxFeat) return CSX_ERR_BAD_ARGS;
+        ng = nf - 1 - kNQuad;
+    }
     if (ldg < ng) return CSX_ERR_BAD_ARGS;
     return CSX_OK;
 }
+
+bool is_full(int nf) { return nf == kFullFeat; }
 
 int row_grid(int64_t n) {
     const int64_t tiles = (n + kRowThreads - 1) / kRowThreads;
@@ -470,14 +545,19 @@ int row_grid(int64_t n) {
 
 size_t tile_bytes(int ng) { return static_cast<size_t>(kRowThreads) * stride_for(ng) * sizeof(float); }
 
-constexpr size_t kPartCoefBytes = static_cast<size_t>(kPartBlocks) * kMaxFeat * sizeof(double);
-constexpr size_t kPartGramBytes = static_cast<size_t>(kPartBlocks) * kGramPairs * kGramBlk * kGramBlk * sizeof(double);
-constexpr size_t kGramSmem = static_cast<size_t>(kGramRows) * kGramFeatPad * sizeof(double);
+int gram_parts(int nf) { return is_full(nf) ? kPartBlocksFull : kPartBlocks; }
+size_t part_gram_bytes(int nf) {
+    return static_cast<size_t>(gram_parts(nf)) * gram_pairs(nf) * kGramBlk * kGramBlk * sizeof(double);
+}
+constexpr size_t kPartCoefBytes = static_cast<size_t>(kPartBlocks) * kFeatCap * sizeof(double);
+size_t gram_smem(int nf) { return static_cast<size_t>(kGramRows) * gram_nb(nf) * kGramBlk * sizeof(double); }
 constexpr size_t kSolveSmem = (static_cast<size_t>(tri(kMaxFeat)) + kMaxFeat) * sizeof(double);
 
-int enable_solve_smem() {  // on the current device, every call (cheap)
+int enable_smem() {  // on the current device, every call (cheap)
     SG_CUDA(cudaFuncSetAttribute(sg_ridge_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(kSolveSmem)));
+    SG_CUDA(cudaFuncSetAttribute(sg_gram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(gram_smem(kFullFeat))));
     return CSX_OK;
 }
 
@@ -493,7 +573,7 @@ int coef_grad(int ng, int nf, const float *genes, int64_t n, int ldg, const TG *
                                             : 1);
     sg_grad_coef_kernel<TG><<<grid, kRowThreads, tile_bytes(ng), s>>>(ng, nf, genes, n, ldg, gout, part);
     SG_CUDA(cudaGetLastError());
-    sg_sum_parts_kernel<<<1, 256, 0, s>>>(part, grid, kMaxFeat, nf, dcoef);
+    sg_sum_parts_kernel<<<(nf + 255) / 256, 256, 0, s>>>(part, grid, kFeatCap, nf, dcoef);
     SG_CUDA(cudaGetLastError());
     return CSX_OK;
 }
@@ -503,8 +583,8 @@ int coef_grad(int ng, int nf, const float *genes, int64_t n, int ldg, const TG *
 extern "C" {
 
 uint64_t csx_sg_workspace_bytes(int nf) {
-    (void)nf;
-    return static_cast<uint64_t>(kPartGramBytes + kPartCoefBytes);
+    const size_t g = is_full(nf) ? part_gram_bytes(kFullFeat) : part_gram_bytes(kMaxFeat);
+    return static_cast<uint64_t>(g + kPartCoefBytes);
 }
 
 int csx_sg_forward(const float *d_coef, int nf, const float *d_genes, int64_t n, int ldg, int precision,
@@ -515,10 +595,19 @@ int csx_sg_forward(const float *d_coef, int nf, const float *d_genes, int64_t n,
     if (!d_coef || !d_genes || !d_score) return CSX_ERR_BAD_ARGS;
     auto s = static_cast<cudaStream_t>(stream);
     const int grid = row_grid(n);
+    const size_t tb = tile_bytes(ng);
     if (precision == CSX_SG_FP32) {
-        sg_forward_kernel<CSX_SG_FP32><<<grid, kRowThreads, tile_bytes(ng), s>>>(d_coef, ng, d_genes, n, ldg, d_score);
+        if (is_full(nf))
+            sg_forward_kernel<CSX_SG_FP32, kMaxLin><<<grid, kRowThreads, tb, s>>>(d_coef, ng, d_genes, n, ldg, d_score);
+        else
+            sg_forward_kernel<CSX_SG_FP32, kQuadGenes><<<grid, kRowThreads, tb, s>>>(d_coef, ng, d_genes, n, ldg,
+                                                                                    d_score);
     } else if (precision == CSX_SG_BF16) {
-        sg_forward_kernel<CSX_SG_BF16><<<grid, kRowThreads, tile_bytes(ng), s>>>(d_coef, ng, d_genes, n, ldg, d_score);
+        if (is_full(nf))
+            sg_forward_kernel<CSX_SG_BF16, kMaxLin><<<grid, kRowThreads, tb, s>>>(d_coef, ng, d_genes, n, ldg, d_score);
+        else
+            sg_forward_kernel<CSX_SG_BF16, kQuadGenes><<<grid, kRowThreads, tb, s>>>(d_coef, ng, d_genes, n, ldg,
+                                                                                    d_score);
     } else {
         return CSX_ERR_BAD_ARGS;
     }
@@ -533,7 +622,12 @@ int csx_sg_forward_f64(const double *d_coef, int nf, const float *d_genes, int64
     if (n == 0) return CSX_OK;
     if (!d_coef || !d_genes || !d_score) return CSX_ERR_BAD_ARGS;
     auto s = static_cast<cudaStream_t>(stream);
-    sg_forward_f64_kernel<<<row_grid(n), kRowThreads, tile_bytes(ng), s>>>(d_coef, ng, d_genes, n, ldg, d_score);
+    if (is_full(nf))
+        sg_forward_f64_kernel<kMaxLin><<<row_grid(n), kRowThreads, tile_bytes(ng), s>>>(d_coef, ng, d_genes, n, ldg,
+                                                                                      d_score);
+    else
+        sg_forward_f64_kernel<kQuadGenes><<<row_grid(n), kRowThreads, tile_bytes(ng), s>>>(d_coef, ng, d_genes, n,
+                                                                                         ldg, d_score);
     SG_CUDA(cudaGetLastError());
     return CSX_OK;
 }
@@ -547,11 +641,19 @@ int csx_sg_backward(const float *d_coef, int nf, const float *d_genes, int64_t n
     auto s = static_cast<cudaStream_t>(stream);
     if (d_dgenes && n > 0) {
         const int grid = row_grid(n);
-        if (precision == CSX_SG_FP32)
-            sg_grad_genes_kernel<CSX_SG_FP32><<<grid, kRowThreads, tile_bytes(ng), s>>>(d_coef, ng, d_genes, n, ldg,
+        const size_t tb = tile_bytes(ng);
+        const bool full = is_full(nf);
+        if (precision == CSX_SG_FP32 && full)
+            sg_grad_genes_kernel<CSX_SG_FP32, kMaxLin><<<grid, kRowThreads, tb, s>>>(d_coef, ng, d_genes, n, ldg,
+                                                                                    d_gout, d_dgenes);
+        else if (precision == CSX_SG_FP32)
+            sg_grad_genes_kernel<CSX_SG_FP32, kQuadGenes><<<grid, kRowThreads, tb, s>>>(d_coef, ng, d_genes, n, ldg,
                                                                                        d_gout, d_dgenes);
+        else if (full)
+            sg_grad_genes_kernel<CSX_SG_BF16, kMaxLin><<<grid, kRowThreads, tb, s>>>(d_coef, ng, d_genes, n, ldg,
+                                                                                    d_gout, d_dgenes);
         else
-            sg_grad_genes_kernel<CSX_SG_BF16><<<grid, kRowThreads, tile_bytes(ng), s>>>(d_coef, ng, d_genes, n, ldg,
+            sg_grad_genes_kernel<CSX_SG_BF16, kQuadGenes><<<grid, kRowThreads, tb, s>>>(d_coef, ng, d_genes, n, ldg,
                                                                                        d_gout, d_dgenes);
         SG_CUDA(cudaGetLastError());
     }
@@ -571,21 +673,24 @@ int csx_sg_normal_equations(int nf, const float *d_genes, int64_t n, int ldg, co
     int ng = 0;
     if (int rc = check_layout(nf, ldg, n, ng)) return rc;
     if (!d_gram || !d_work || (n > 0 && !d_genes) || (d_fit && !d_rhs)) return CSX_ERR_BAD_ARGS;
+    if (int rc = enable_smem()) return rc;
     auto s = static_cast<cudaStream_t>(stream);
     auto *part_g = static_cast<double *>(d_work);
-    auto *part_r = reinterpret_cast<double *>(static_cast<char *>(d_work) + kPartGramBytes);
-    const int nb = (nf + kGramBlk - 1) / kGramBlk;
-    const int npairs = nb * (nb + 1) / 2;
-    const int threads = ((npairs > nf ? npairs : nf) + 31) / 32 * 32;
+    auto *part_r = reinterpret_cast<double *>(static_cast<char *>(d_work) + part_gram_bytes(is_full(nf) ? kFullFeat
+                                                                                                          : kMaxFeat));
+    const int npairs = gram_pairs(nf);
+    const int ycols = (npairs + kGramThreads - 1) / kGramThreads;
+    const int threads = ycols > 1 ? kGramThreads : ((npairs > nf ? npairs : nf) + 31) / 32 * 32;
     const int64_t want = (n + kGramRows - 1) / kGramRows;
-    const int grid = static_cast<int>(want < kPartBlocks ? (want > 0 ? want : 1) : kPartBlocks);
-    sg_gram_kernel<<<grid, threads, kGramSmem, s>>>(ng, nf, d_genes, n, ldg, d_fit, part_g, part_r);
+    const int cap = gram_parts(nf);
+    const int grid = static_cast<int>(want < cap ? (want > 0 ? want : 1) : cap);
+    sg_gram_kernel<<<dim3(grid, ycols), threads, gram_smem(nf), s>>>(ng, nf, d_genes, n, ldg, d_fit, part_g, part_r);
     SG_CUDA(cudaGetLastError());
-    const int ne = npairs * kGramBlk * kGramBlk;
-    sg_gram_sum_kernel<<<(ne + 255) / 256, 256, 0, s>>>(part_g, grid, nf, d_gram);
+    const int64_t ne = static_cast<int64_t>(npairs) * kGramBlk * kGramBlk;
+    sg_gram_sum_kernel<<<static_cast<unsigned>((ne + 255) / 256), 256, 0, s>>>(part_g, grid, nf, d_gram);
     SG_CUDA(cudaGetLastError());
     if (d_fit) {
-        sg_sum_parts_kernel<<<1, 256, 0, s>>>(part_r, grid, kMaxFeat, nf, d_rhs);
+        sg_sum_parts_kernel<<<(nf + 255) / 256, 256, 0, s>>>(part_r, grid, kFeatCap, nf, d_rhs);
         SG_CUDA(cudaGetLastError());
     }
     return CSX_OK;
@@ -593,12 +698,24 @@ int csx_sg_normal_equations(int nf, const float *d_genes, int64_t n, int ldg, co
 
 int csx_sg_ridge_solve(int nf, const double *d_gram, const double *d_rhs, double alpha, const double *d_prior,
                        double *d_w, int *d_status, void *stream) {
-    if (nf < 1 || nf > kMaxFeat || !d_gram || !d_rhs || !d_w || !d_status || !(alpha >= 0.0)) return CSX_ERR_BAD_ARGS;
-    if (int rc = enable_solve_smem()) return rc;
-    const size_t smem = (static_cast<size_t>(tri(nf)) + nf) * sizeof(double);
-    sg_ridge_solve_kernel<<<1, kSolveThreads, smem, static_cast<cudaStream_t>(stream)>>>(nf, d_gram, d_rhs, alpha,
-                                                                                        d_prior, d_w, d_status);
-    SG_CUDA(cudaGetLastError());
+    if (nf < 1 || (nf > kMaxFeat && nf != kFullFeat) || !d_gram || !d_rhs || !d_w || !d_status || !(alpha >= 0.0))
+        return CSX_ERR_BAD_ARGS;
+    if (int rc = enable_smem()) return rc;
+    auto s = static_cast<cudaStream_t>(stream);
+    const size_t bytes = (static_cast<size_t>(tri(nf)) + nf) * sizeof(double);
+    if (nf <= kMaxFeat) {
+        sg_ridge_solve_kernel<<<1, kSolveThreads, bytes, s>>>(nf, d_gram, d_rhs, alpha, d_prior, d_w, d_status);
+        SG_CUDA(cudaGetLastError());
+        return CSX_OK;
+    }
+    // the full surface: the factor does not fit in shared memory
+    void *scratch = nullptr;
+    SG_CUDA(cudaMallocAsync(&scratch, bytes, s));
+    sg_ridge_solve_global_kernel<<<1, kSolveThreads, 0, s>>>(nf, d_gram, d_rhs, alpha, d_prior, d_w, d_status,
+                                                             static_cast<double *>(scratch));
+    const cudaError_t e = cudaGetLastError();
+    SG_CUDA(cudaFreeAsync(scratch, s));
+    SG_CUDA(e);
     return CSX_OK;
 }
 
@@ -610,8 +727,12 @@ int csx_sg_ascend(const float *d_coef, int nf, float *d_genes, int64_t n, int ld
     if (n == 0) return CSX_OK;
     if (!d_coef || !d_genes) return CSX_ERR_BAD_ARGS;
     auto s = static_cast<cudaStream_t>(stream);
-    sg_ascend_kernel<<<row_grid(n), kRowThreads, tile_bytes(ng), s>>>(d_coef, ng, d_genes, n, ldg, eta, steps,
-                                                                     d_score);
+    if (is_full(nf))
+        sg_ascend_kernel<kMaxLin><<<row_grid(n), kRowThreads, tile_bytes(ng), s>>>(d_coef, ng, d_genes, n, ldg, eta,
+                                                                                 steps, d_score);
+    else
+        sg_ascend_kernel<kQuadGenes><<<row_grid(n), kRowThreads, tile_bytes(ng), s>>>(d_coef, ng, d_genes, n, ldg,
+                                                                                    eta, steps, d_score);
     SG_CUDA(cudaGetLastError());
     return CSX_OK;
 }

@@ -11,8 +11,10 @@ gradient 2Φᵀ(Φw − y) + 2α(w − w₀) from the backward kernel, which van
 at the solution.
 
 Coefficients use the compact layout of brain/evolve.py:211-220: nf = 1 + ng +
-136 (153 for 16 genes, 166 for 29). Every tensor must live on a CUDA device;
-there is no CPU path.
+136 (153 for 16 genes, 166 for 29), or the full surface's nf = 465 (all 29
+genes quadratic: the quad-block extension docs/RESEARCH_V05C.md:99-102
+queues; its FP32 forward is the screen's csx_score_full order). Every tensor
+must live on a CUDA device; there is no CPU path.
 """
 from __future__ import annotations
 
@@ -24,6 +26,7 @@ from . import _lib
 from ._lib import SG_BF16, SG_FP32, SG_FP64, check, lib
 
 NQUAD = 136
+FULL_NF = _lib.FULL_NF  # 465
 
 
 def _ptr(t: Optional[torch.Tensor]) -> Optional[int]:
@@ -43,14 +46,16 @@ def _genes(genes: torch.Tensor) -> torch.Tensor:
 
 
 def _ng(nf: int) -> int:
+    if nf == FULL_NF:
+        return 29
     ng = nf - 1 - NQUAD
     if not 16 <= ng <= 29:
-        raise ValueError(f"nf={nf}: the compact layout has 153..166 coefficients")
+        raise ValueError(f"nf={nf}: the compact layouts have 153..166 or 465 coefficients")
     return ng
 
 
-def workspace(device) -> torch.Tensor:
-    return torch.empty(int(lib().csx_sg_workspace_bytes(166)), dtype=torch.uint8, device=device)
+def workspace(device, nf: int = 166) -> torch.Tensor:
+    return torch.empty(int(lib().csx_sg_workspace_bytes(int(nf))), dtype=torch.uint8, device=device)
 
 
 class _Score(torch.autograd.Function):
@@ -75,7 +80,7 @@ class _Score(torch.autograd.Function):
         want_g, want_c = ctx.needs_input_grad[0], ctx.needs_input_grad[1]
         dgenes = torch.empty_like(genes) if want_g else None
         dcoef = torch.empty(coef_c.numel(), dtype=torch.float64, device=genes.device) if want_c else None
-        work = workspace(genes.device) if want_c else None
+        work = workspace(genes.device, coef_c.numel()) if want_c else None
         check(lib().csx_sg_backward(coef_c.data_ptr(), coef_c.numel(), genes.data_ptr(), genes.shape[0],
                                     genes.stride(0), ctx.precision, gout.data_ptr(), _ptr(dgenes), _ptr(dcoef),
                                     _ptr(work), _stream(genes.device)), "sg_backward")
@@ -111,7 +116,7 @@ def normal_equations(genes: torch.Tensor, fit: Optional[torch.Tensor], nf: int):
     gram = torch.empty((nf, nf), dtype=torch.float64, device=dev)
     rhs = torch.empty(nf, dtype=torch.float64, device=dev) if fit is not None else None
     y = fit.detach().to(device=dev, dtype=torch.float64).contiguous() if fit is not None else None
-    work = workspace(dev)
+    work = workspace(dev, nf)
     check(lib().csx_sg_normal_equations(nf, genes.data_ptr(), genes.shape[0], genes.stride(0), _ptr(y),
                                         gram.data_ptr(), _ptr(rhs), work.data_ptr(), _stream(dev)),
           "sg_normal_equations")
@@ -119,7 +124,8 @@ def normal_equations(genes: torch.Tensor, fit: Optional[torch.Tensor], nf: int):
 
 
 def ridge_solve(gram: torch.Tensor, rhs: torch.Tensor, alpha: float, prior: Optional[torch.Tensor] = None):
-    """w = (G + αI)⁻¹ (rhs + α·prior), FP64 Cholesky on one CTA."""
+    """w = (G + αI)⁻¹ (rhs + α·prior), FP64 Cholesky on one CTA (the factor in
+    shared memory up to 166 coefficients, in a global scratch for 465)."""
     nf = gram.shape[0]
     dev = gram.device
     gram = gram.to(torch.float64).contiguous()
@@ -156,7 +162,7 @@ def ridge_grad(genes: torch.Tensor, fit: torch.Tensor, w: torch.Tensor, prior: t
     resid = score_f64(genes, w) - fit.detach().to(device=dev, dtype=torch.float64)
     resid = resid.contiguous()
     g = torch.empty(nf, dtype=torch.float64, device=dev)
-    work = workspace(dev)
+    work = workspace(dev, nf)
     check(lib().csx_sg_backward_coef_f64(nf, genes.data_ptr(), genes.shape[0], genes.stride(0), resid.data_ptr(),
                                          g.data_ptr(), work.data_ptr(), _stream(dev)), "sg_backward_coef_f64")
     pr = prior.detach().to(device=dev, dtype=torch.float64)

@@ -304,3 +304,95 @@ def test_bad_arguments():
         surrogate.score(torch.zeros((4, 29)), torch.zeros(166))
     with pytest.raises(_lib.CsxError):
         surrogate.score(torch.zeros((4, 20), device="cuda"), torch.zeros(166, device="cuda"))
+
+
+# ---- the full surface (465 coefficients: all 29 genes quadratic) ---------------------
+
+def _full_case(n, seed, scale=1.0):
+    rng = np.random.default_rng(seed)
+    genes = rng.random((n, 29), dtype=np.float32)
+    coef = (rng.normal(0, 1, 465) * scale).astype(np.float32)
+    return genes, coef
+
+
+def test_full_forward_is_the_screen_score():
+    """The FP32 forward of the full layout evaluates csx_score_full's FMA
+    order: bit-equal to the screen's score of the same genes, and within the
+    FP32 bound of the FP64 oracle."""
+    import refit
+    import torch
+
+    from codec_arena_gb300 import screen, surrogate
+
+    genes, coef = _full_case(4000, 1)
+    d_g = torch.from_numpy(genes).cuda()
+    got = surrogate.score(d_g, torch.from_numpy(coef).cuda()).cpu().numpy()
+    scr = screen.score_genes(screen.ModelFull.from_compact(coef), d_g).cpu().numpy()
+    np.testing.assert_array_equal(got.view(np.uint32), scr.view(np.uint32))
+    X = np.abs(refit.features(genes, full=True))
+    assert np.all(np.abs(got - refit.score(genes, coef)) <= 1e-5 * (X @ np.abs(coef.astype(np.float64))))
+    g64 = surrogate.score_f64(d_g, torch.from_numpy(coef.astype(np.float64)).cuda()).cpu().numpy()
+    np.testing.assert_allclose(g64, refit.score(genes, coef), rtol=1e-12, atol=1e-12)
+
+
+def test_full_gene_gradient_and_coefficient_gradient():
+    import refit
+    import torch
+
+    from codec_arena_gb300 import surrogate
+
+    genes, coef = _full_case(3000, 2)
+    g = torch.from_numpy(genes).cuda().requires_grad_(True)
+    c = torch.from_numpy(coef.astype(np.float64)).cuda().requires_grad_(True)
+    s = surrogate.score(g, c)
+    gout = torch.from_numpy(np.random.default_rng(3).normal(size=3000).astype(np.float32)).cuda()
+    (s * gout).sum().backward()
+    want_g = refit.grad_genes(genes, coef) * gout.cpu().numpy()[:, None].astype(np.float64)
+    scale = np.abs(refit.grad_genes(genes, np.abs(coef))).max()
+    assert np.abs(g.grad.cpu().numpy() - want_g).max() <= 1e-5 * scale * np.abs(gout.cpu().numpy()).max()
+    want_c = refit.features(genes, full=True).T @ gout.cpu().numpy().astype(np.float64)
+    np.testing.assert_allclose(c.grad.cpu().numpy(), want_c, rtol=1e-9, atol=1e-9 * np.abs(want_c).max())
+
+
+def test_full_normal_equations_and_refit():
+    """465 features: ΦᵀΦ spans 6903 4x4 blocks over seven CTA columns; the
+    Cholesky factor (108k entries) lives in a global scratch."""
+    import refit
+    import torch
+
+    from codec_arena_gb300 import surrogate
+
+    rng = np.random.default_rng(7)
+    n = 60000
+    genes = rng.random((n, 29), dtype=np.float32)
+    w_true = rng.normal(0, 1, 465)
+    fit = refit.features(genes, full=True) @ w_true + rng.standard_t(3, n) * 0.5
+    d_g, d_y = torch.from_numpy(genes).cuda(), torch.from_numpy(fit).cuda()
+    G, r = surrogate.normal_equations(d_g, d_y, 465)
+    Gw, rw = refit.normal_equations(genes, fit, full=True)
+    np.testing.assert_allclose(G.cpu().numpy(), Gw, rtol=1e-12)
+    X = np.abs(refit.features(genes, full=True))
+    assert np.all(np.abs(r.cpu().numpy() - rw) <= 1e-12 * (X.T @ np.abs(fit)))
+    G2, _ = surrogate.normal_equations(d_g, d_y, 465)
+    assert torch.equal(G, G2)
+    prior = rng.normal(0, 0.1, 465)
+    w = surrogate.refit(d_g, d_y, torch.from_numpy(prior).cuda(), alpha=1e-2).cpu().numpy()
+    want = refit.refit_cholesky(genes, fit, prior, 1e-2)
+    assert np.abs(w - want).max() <= 1e-8 * np.abs(want).max()
+    assert np.abs(w - w_true).max() < 0.5  # the fit recovers the surface
+
+
+def test_full_ascent_raises_the_score():
+    import torch
+
+    from codec_arena_gb300 import surrogate
+
+    genes, coef = _full_case(2000, 5, 0.2)
+    d_c = torch.from_numpy(coef).cuda()
+    d_g = torch.from_numpy(genes).cuda()
+    before = surrogate.score(d_g, d_c)
+    new, after = surrogate.ascend(d_g, d_c, 1e-3, 10)
+    assert (after >= before - 1e-4).float().mean().item() > 0.99
+    assert after.mean().item() > before.mean().item()
+    assert float(new.min()) >= 0.0 and float(new.max()) <= 1.0
+    np.testing.assert_array_equal(after.cpu().numpy(), surrogate.score(new, d_c).detach().cpu().numpy())
