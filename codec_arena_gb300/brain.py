@@ -11,8 +11,12 @@ result then equals the file-based path exactly.
 
 The format helpers mirror evolve.py's own: `load_pop` (:71-101),
 `genome_line` (:104-106), `features` (:211-220), `load_weights` (:223-241),
-`save_weights` (:244-247); the search-counter bookkeeping mirrors
-`screens_count.txt` (:621-622) and its merge in tools/merge_results.py:62-124.
+`save_weights` (:244-247); `refit_surrogate` (:250-268) runs on the GPU. The
+search-counter bookkeeping mirrors `screens_count.txt` (:621-622) and its
+merge in tools/merge_results.py:62-124. `features_full`, `extend_to_full` and
+the 465-coefficient weights that screen_generation / refit_surrogate accept
+are the full quadratic surface (all 29 genes), which the reference queues in
+docs/RESEARCH_V05C.md:99-102 but does not implement.
 """
 from __future__ import annotations
 
@@ -73,8 +77,39 @@ def features(genes) -> np.ndarray:
     return np.concatenate([np.ones((g.shape[0], 1)), g, quad], axis=1)
 
 
+FULL_NF = 465  # the full surface: all 29 genes quadratic (csx_screen.h)
+
+
+def features_full(genes) -> np.ndarray:
+    """The full surface's features: (n, 29) genes -> (n, 465)
+    [1 | 29 linear | g_i g_j for j <= i < 29], the pattern of features()
+    with the quadratic block over every gene (the extension
+    docs/RESEARCH_V05C.md:99-102 queues; no reference code)."""
+    g = np.atleast_2d(np.asarray(genes, dtype=np.float64))
+    ii, jj = np.tril_indices(29)
+    return np.concatenate([np.ones((g.shape[0], 1)), g, g[:, ii] * g[:, jj]], axis=1)
+
+
+def extend_to_full(w: Sequence[float]) -> List[float]:
+    """A 166-coefficient model (any layout after load_weights) as the same
+    surface in the full layout: the quadratic block over genes 0..15 placed in
+    the 29-gene triangle, the new pairs 0, and the intercept times 16 (the
+    reference's Model.score counts w0 in each of its 16 lanes)."""
+    w = [float(x) for x in w]
+    if len(w) != 166:
+        raise ValueError("extend_to_full takes the 166-coefficient layout")
+    full = [16.0 * w[0]] + w[1:30]
+    q = 30
+    for i in range(29):
+        for j in range(i + 1):
+            full.append(w[q] if i < 16 else 0.0)
+            q += 1 if i < 16 else 0
+    return full
+
+
 def load_weights(path: str) -> List[float]:
-    """brain/evolve.py:223-241: any compact layout migrated to 166."""
+    """brain/evolve.py:223-241: any compact layout migrated to 166. A file of
+    465 coefficients holds the full surface and is returned as it is."""
     with open(path) as f:
         toks = f.read().split()
     n = int(toks[0])
@@ -117,11 +152,13 @@ def screen_generation(elites: Sequence[Dict], model, *, screens: int, keep: int,
                       v6_fix: bool = False) -> Tuple[List[Dict], int]:
     """One generation's screen as brain/evolve.py:431-454 runs it, in process.
 
-    `model` is a screen.Model or compact weights. Returns (promoted, screened):
-    promoted dicts carry pa, pb, tribe and the 29 genes, best first.
+    `model` is a screen.Model, a screen.ModelFull or compact weights (465 of
+    them: the full surface). Returns (promoted, screened): promoted dicts
+    carry pa, pb, tribe and the 29 genes, best first.
     """
-    if not isinstance(model, _screen.Model):
-        model = _screen.Model.from_compact(np.asarray(model, dtype=np.float32))
+    if not isinstance(model, (_screen.Model, _screen.ModelFull)):
+        w = np.asarray(model, dtype=np.float32)
+        model = _screen.ModelFull.from_compact(w) if w.shape[0] == FULL_NF else _screen.Model.from_compact(w)
     sigma = 0.12 * (sigma_decay ** gen)
     if text_roundtrip:  # evolve.py passes sigma as "%.4f" text
         sigma = float(f"{sigma:.4f}")
@@ -136,6 +173,30 @@ def screen_generation(elites: Sequence[Dict], model, *, screens: int, keep: int,
         promoted.append({"id": 0, "gen": 0, "pa": int(r["pa"]), "pb": int(r["pb"]), "tribe": int(r["tribe"]),
                          "g": g})
     return promoted, screened
+
+
+def refit_surrogate(rows, prior_w: Sequence[float], out_path: str, alpha: float = 50.0) -> bool:
+    """brain/evolve.py:250-268 on the GPU: ridge refit toward the prior,
+    min ||Xw - y||² + α||w - w_prior||², normal equations and Cholesky in
+    FP64. rows: (genes, fit) pairs. As the reference: False (nothing written)
+    below 300 rows or when the prior's length is not the feature count; here
+    the prior may also hold the full surface's 465 coefficients."""
+    import torch
+
+    from . import surrogate as _sg
+
+    if len(rows) < 300:
+        return False
+    prior = np.asarray(prior_w, dtype=np.float64)
+    if prior.shape[0] not in (166, FULL_NF):
+        return False
+    genes = torch.tensor(np.array([list(g) for g, _ in rows], dtype=np.float32), device="cuda")
+    fit = torch.tensor(np.array([f for _, f in rows], dtype=np.float64), device="cuda")
+    if genes.shape[1] != 29:
+        return False
+    w = _sg.refit(genes, fit, torch.from_numpy(prior).cuda(), alpha=alpha)
+    save_weights(out_path, [float(v) for v in w.cpu().numpy()])
+    return True
 
 
 def next_population(elites: Sequence[Dict], promoted: Sequence[Dict], *, shard: int, gen: int, pop: int,

@@ -188,3 +188,81 @@ def test_search_counter_bookkeeping(tmp_path):
     assert st["search_milestones"] == {"1e6": "run 5", "1e9": "run 5"}
     st2 = brain.update_lifetime_counters(str(tmp_path), st)
     assert st2["milestones"] == {"1e5": "run 5"} and st2["runs"] == 6
+
+
+def test_extend_to_full_is_the_same_surface(orc):
+    """A 166-coefficient model moved into the full layout scores every genome
+    as the reference's Model.score surface does (16·w0 intercept), in FP64."""
+    from codec_arena_gb300 import brain
+
+    rng = np.random.default_rng(5)
+    w = rng.normal(size=166).astype(np.float32)
+    full = np.asarray(brain.extend_to_full(w), dtype=np.float64)
+    assert full.shape == (465,)
+    m = orc.model_from_compact(w)
+    mf = orc.model_full_from_compact(full.astype(np.float32))
+    for _ in range(10):
+        g = rng.random(29).astype(np.float32)
+        want = orc.score_f64(m, g)
+        assert abs(float(brain.features_full(g)[0] @ full) - want) < 1e-9 * (1 + abs(want))
+        assert abs(orc.score_f64(mf, g) - want) < 1e-9 * (1 + abs(want))
+
+
+def test_load_weights_keeps_the_full_layout(tmp_path):
+    from codec_arena_gb300 import brain
+
+    w = [float(i) / 7 for i in range(465)]
+    p = tmp_path / "w.txt"
+    brain.save_weights(str(p), w)
+    got = brain.load_weights(str(p))
+    assert len(got) == 465 and np.allclose(got, w, rtol=1e-8)
+
+
+@pytest.mark.gpu
+def test_refit_surrogate_on_the_gpu(csx, tmp_path):
+    """brain/evolve.py:250-268's semantics (False below 300 rows or for a
+    prior of the wrong length) and its solution, for the 166 layout and the
+    full 465 one, against the FP64 oracle."""
+    import sys
+
+    from conftest import ROOT, has_gpu
+
+    if not has_gpu():
+        pytest.skip("no CUDA device")
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import refit
+
+    from codec_arena_gb300 import brain
+
+    rng = np.random.default_rng(8)
+    genes = rng.random((4000, 29)).astype(np.float32)
+    fit = rng.normal(size=4000)
+    rows = [(list(map(float, g)), float(f)) for g, f in zip(genes, fit)]
+    out = tmp_path / "surrogate.txt"
+    assert not brain.refit_surrogate(rows[:299], [0.0] * 166, str(out))
+    assert not brain.refit_surrogate(rows, [0.0] * 153, str(out))
+    for nf, full in ((166, False), (465, True)):
+        prior = rng.normal(0, 0.1, nf)
+        assert brain.refit_surrogate(rows, prior, str(out), alpha=50.0)
+        got = np.asarray(brain.load_weights(str(out)))
+        X = refit.features(genes, full=full)
+        want = np.linalg.solve(X.T @ X + 50.0 * np.eye(nf), X.T @ fit + 50.0 * prior)
+        # save_weights writes 9 significant digits
+        np.testing.assert_allclose(got, want, rtol=2e-8, atol=1e-9 * np.abs(want).max())
+
+
+@pytest.mark.gpu
+def test_screen_generation_with_full_weights(csx):
+    from conftest import has_gpu
+
+    if not has_gpu():
+        pytest.skip("no CUDA device")
+    from codec_arena_gb300 import brain, parallel, screen
+
+    elites = _evolve_elites()
+    w = np.random.default_rng(12).normal(0, 0.3, 465).astype(np.float32)
+    got, n = brain.screen_generation(elites, w, screens=200_000, keep=32, seed=3, shard=0, gen=1)
+    cfg = screen.Cfg(200_000, 32, parallel.island_seed(3, 0, 1), threads=4, sigma=0.12 * 0.93)
+    want, m = screen.screen(cfg, screen.ModelFull.from_compact(w), brain.elites_array(elites))
+    assert n == m == 200_000
+    np.testing.assert_array_equal(np.asarray([p["g"] for p in got], dtype=np.float32), want["g"])
