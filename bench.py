@@ -23,7 +23,9 @@ line's value is the plain FP32 fused screen (the reference's own f32
 semantics, bit-exact), and precision_forms carries the BF16 / FP16 values.
 `--workload precision` prints a line whose value is the BF16 form;
 `--workload islands` the batched-islands workload, `--workload refit` the
-GPU ridge refit and the surrogate's forward / backward kernels.
+GPU ridge refit and the surrogate's forward / backward kernels (with the full
+29-gene surface's refit beside it), `--workload full` the generation screened
+on the full 29-gene quadratic surface.
 
 `--impl reference` times the reference's CPU implementation of the path (the
 restatement: Zig is not available) on the same workload, rank 0 only.
@@ -68,7 +70,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-precision", action="store_true", help="skip the tensor-core precision forms")
-    ap.add_argument("--workload", default="generation", choices=["generation", "islands", "precision", "refit"],
+    ap.add_argument("--workload", default="generation",
+                    choices=["generation", "islands", "precision", "refit", "full"],
                     help="islands: 20 islands batched in one graph launch (not the headline line)")
     ap.add_argument("--islands", type=int, default=20)
     ap.add_argument("--islands-scale", type=float, default=1.0,
@@ -512,6 +515,94 @@ def run_refit(args):
                               "speedup": cpu_s * 1000 / ms_refit},
             "surrogate_rows_per_s": {"forward": n / (ms_fwd * 1e-3), "forward_backward": n / (ms_fwd_bwd * 1e-3)},
             "clocks": clocks, "gpu_launches": 4 * args.steps}
+    line["full_surface"] = refit_full(args, timed, dfma.value)
+    print(json.dumps(line), flush=True)
+
+
+def refit_full(args, timed, dfma):
+    """The same refit on the full surface: 400,000 rows of 29 genes, 465
+    features (all pairs), against numpy FP64 on the host."""
+    import numpy as np
+    import torch
+
+    import refit as orc_refit
+
+    from codec_arena_gb300 import surrogate, workloads as wl
+
+    genes, fit, w_true = wl.refit_table_full()
+    n, nf, alpha = genes.shape[0], 465, 1e-2
+    d_g, d_y = torch.from_numpy(genes).cuda(), torch.from_numpy(fit).cuda()
+    prior = torch.zeros(nf, dtype=torch.float64, device="cuda")
+    ms_refit = timed(lambda: surrogate.refit(d_g, d_y, prior, alpha))
+    ms_gram = timed(lambda: surrogate.normal_equations(d_g, d_y, nf))
+    G, r = surrogate.normal_equations(d_g, d_y, nf)
+    ms_solve = timed(lambda: surrogate.ridge_solve(G, r, alpha, prior))
+    w = surrogate.refit(d_g, d_y, prior, alpha).cpu().numpy()
+    t0 = time.perf_counter()
+    w_np = orc_refit.refit_solve(genes, fit, np.zeros(nf), alpha)
+    cpu_s = time.perf_counter() - t0
+    gram_flop = 2.0 * n * (nf * (nf + 1) / 2 + nf)
+    return {"rows": n, "features": nf, "alpha": alpha, "ms": ms_refit,
+            "stages_ms": {"normal_equations": ms_gram, "cholesky_solve": ms_solve},
+            "roofline": {"bound": "fp64", "kernel": "sg_gram_kernel", "achieved": gram_flop / (ms_gram * 1e-3) / 1e12,
+                         "peak": 2 * dfma / 1e12, "unit": "TFLOP/s",
+                         "frac": gram_flop / (ms_gram * 1e-3) / (2 * dfma) if dfma else None},
+            "vs_numpy_fp64": {"max_abs_diff": float(np.abs(w - w_np).max()), "max_abs_w": float(np.abs(w_np).max()),
+                              "numpy_seconds": cpu_s, "speedup": cpu_s * 1000 / ms_refit},
+            "max_abs_err_vs_truth": float(np.abs(w - w_true).max())}
+
+
+def run_full(args):
+    """`--workload full`: the generation workload screened on the full
+    quadratic surface (all 29 genes; the committed v3 surrogate moved into the
+    465-coefficient layout, new pairs 0): candidates/s by CUDA events, L2
+    flushed between steps, and the issue roofline at its algorithmic work
+    (1235 RNG + 145 gene + 2 x 464 FMA lane-ops per candidate)."""
+    import numpy as np
+    import torch
+
+    from codec_arena_gb300 import _lib, brain, screen, workloads as wl
+
+    torch.cuda.set_device(0)
+    el = wl.seeded_elites(N_ELITES)
+    model = screen.ModelFull.from_compact(
+        np.asarray(brain.extend_to_full(brain.migrate_weights(wl.surrogate_161())), dtype=np.float32))
+    cfg = screen.Cfg(args.lam, args.keep, SEED, threads=args.threads, flags=_lib.FLAG_STAGE_TIMES)
+    d_el = torch.from_numpy(el.view(np.uint8).copy()).cuda()
+    d_out = torch.zeros(args.keep * _lib.SURVIVOR_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    d_res = torch.zeros(4, dtype=torch.int64, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(max(3, args.warmup)):
+        screen.screen_device(cfg, model, d_el, d_out, d_res)
+    torch.cuda.synchronize()
+    res = d_res.cpu().numpy()
+    assert res[2] == 0 and res[1] == args.lam, f"device result {res}"
+    sampler = ClockSampler(0)
+    sampler.start()
+    ms, kms = [], []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        screen.screen_device(cfg, model, d_el, d_out, d_res)
+        b.record()
+        b.synchronize()
+        ms.append(a.elapsed_time(b))
+        kms.append(screen.last_run_info()["ms_screen"])
+    clocks = sampler.stop()
+    info = screen.last_run_info()
+    ops = 1235 + 145 + 2 * 464
+    achieved = args.lam / (statistics.mean(kms) * 1e-3) * ops / 1e12
+    line = {"metric": "candidates/sec, full 29-gene quadratic surface, 1 GB300", "value":
+            args.lam / (statistics.mean(ms) / 1000), "unit": "candidates/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": statistics.mean(ms), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64/f32", "data": "synthetic (seeded)",
+            "config": dict(workload_config(args, 1), surrogate="state/surrogate.txt (v3, 161) in the full "
+                           "465-coefficient layout, new pairs 0"),
+            "roofline": dict(issue_slots(achieved, clocks), kernel="csx::screen_kernel<true, FullScreenArgs>",
+                             algorithmic_ops_per_candidate=ops, bound="int/fp32-issue"),
+            "stages_ms_last_step": {k: round(v, 4) for k, v in info.items() if k.startswith("ms_")},
+            "clocks": clocks, "gpu_launches": int(info["launches"]) * args.steps}
     print(json.dumps(line), flush=True)
 
 
@@ -519,6 +610,8 @@ def main():
     args = parse()
     if args.workload == "refit" and args.impl != "reference":
         return run_refit(args)
+    if args.workload == "full" and args.impl != "reference":
+        return run_full(args)
     if args.workload == "precision" and args.impl != "reference":
         return run_precision(args)
     if args.impl == "reference":

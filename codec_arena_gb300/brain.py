@@ -113,7 +113,13 @@ def load_weights(path: str) -> List[float]:
     with open(path) as f:
         toks = f.read().split()
     n = int(toks[0])
-    w = [float(x) for x in toks[1:1 + n]]
+    return migrate_weights([float(x) for x in toks[1:1 + n]])
+
+
+def migrate_weights(w: Sequence[float]) -> List[float]:
+    """load_weights' migration of a compact weight list (brain/evolve.py:228-240)."""
+    w = [float(x) for x in w]
+    n = len(w)
     if n == 153:
         w = w[:17] + [0.0] * 13 + w[17:]
     elif n == 159:

@@ -88,6 +88,24 @@ def refit_table(n: int = 400_000, seed: int = 5, ng: int = 16, noise: float = 0.
     return genes, fit, w_true
 
 
+def refit_table_full(n: int = 400_000, seed: int = 6, noise: float = 0.5):
+    """Synthetic refit table for the full surface: n rows of 29 genes uniform
+    in [0, 1] (f32), targets = a seeded quadratic over all 29 genes (465
+    N(0, 1) coefficients, FP64) plus Student-t(3) noise of scale `noise`.
+    Returns (genes, fit, w_true)."""
+    rng = np.random.default_rng(seed)
+    genes = rng.random((n, 29), dtype=np.float32)
+    w_true = rng.normal(0.0, 1.0, 465)
+    g = genes.astype(np.float64)
+    ii, jj = np.tril_indices(29)
+    fit = w_true[0] + g @ w_true[1:30]
+    for a in range(0, n, 50_000):  # the 435 products in row blocks (bounded host memory)
+        b = min(n, a + 50_000)
+        fit[a:b] += (g[a:b, ii] * g[a:b, jj]) @ w_true[30:]
+    fit = fit + noise * rng.standard_t(3, n)
+    return genes, fit, w_true
+
+
 def seeded_islands(n: int = 20, seed: int = 4, lam_lo: float = 1e8, lam_hi: float = 2.65e9,
                    ne_lo: int = 16, ne_hi: int = 256, keeps=(32, 128, 256), threads: int = 4):
     """Batched-islands workload: n islands with log-uniform budgets in

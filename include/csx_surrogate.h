@@ -16,6 +16,9 @@
  *   [1+ng .. nf)   quadratic terms g_i·g_j over genes 0..15, (i, j <= i),
  *                  i outer, j inner.
  * nf = 153 is the v1 layout (16 genes), 166 the v6 layout (29 genes).
+ * nf = 465 is the full surface of csx_screen.h (CSX_FULL_NF): 29 linear terms
+ * and the quadratic terms over all 29 genes, (i, j <= i), i outer; its FP32
+ * forward evaluates csx_score_full's FMA order.
  *
  * Genes: n rows of ldg floats (ldg >= ng); only the first ng are read.
  * Every pointer named d_* is device memory; `stream` is a cudaStream_t
@@ -70,7 +73,8 @@ int csx_sg_normal_equations(int nf, const float *d_genes, int64_t n, int ldg, co
 
 /* Ridge solve in FP64 by Cholesky on one CTA: w = (G + αI)⁻¹ (rhs + α·prior).
    d_prior may be NULL (zero prior). d_status (one int) receives 0, or k+1
-   when the k-th pivot is not positive. nf <= 166. */
+   when the k-th pivot is not positive. nf <= 166, or 465 (the factor then
+   lives in a scratch allocated and freed on `stream`). */
 int csx_sg_ridge_solve(int nf, const double *d_gram, const double *d_rhs, double alpha, const double *d_prior,
                        double *d_w, int *d_status, void *stream);
 
