@@ -159,6 +159,53 @@ __device__ __forceinline__ CandHead cand_head(const SynthConst &C, uint64_t seed
     return h;
 }
 
+// Synthesis state of one candidate (src/screen.zig:236-246): the parent rows
+// (row ne, all 0.5, for an immigrant), the mutation constants (an immigrant's
+// 0.5 + (u - 0.5) = u draws its genes uniformly) and the splitmix64 state of
+// gene 0's unit draw; a crossover gene's bit draw precedes its unit draw.
+struct GeneSource {
+    const float *pa, *pb;
+    float B, nb1, B23;
+    uint64_t su, step;
+};
+
+__device__ __forceinline__ GeneSource gene_source(const SynthConst &C, const float *__restrict__ el,
+                                                  uint64_t seed_t, uint64_t p, const CandHead &h) {
+    GeneSource S;
+    const uint64_t s0 = seed_t + (p + 1) * kGolden;
+    S.pa = el + (h.imm ? C.ne : h.ea) * kNtot;
+    S.pb = el + (h.imm ? C.ne : h.eb) * kNtot;
+    S.B = h.imm ? 0.5f : C.sigma;
+    S.nb1 = h.imm ? -0.5f : C.nsig1;
+    S.B23 = h.imm ? 0x1p-24f : C.sigma23;
+    S.step = h.imm ? kGolden : 2 * kGolden;
+    S.su = s0 + (h.imm ? 3ull : 4ull) * kGolden;
+    return S;
+}
+
+// Gene k before the jump: crossover parent, mutation, clamp01 (NaN -> 1, as
+// @min(1, NaN) == 1; the fast form's delta is finite and the elite table holds
+// no NaN, so g is never NaN there). Advances S to the next gene's draws.
+template <bool kFastDelta>
+__device__ __forceinline__ float next_gene(GeneSource &S, int k) {
+    const uint32_t bw = draw_bitword(S.su - kGolden);  // crossover bit draw
+    const uint32_t vh = draw_vh(S.su);                 // unit draw
+    S.su += S.step;
+    const float *src = (static_cast<int32_t>(bw) < 0) ? S.pb : S.pa;
+    const float par = src[k];
+    float g;
+    if (kFastDelta) {
+        g = __fadd_rn(par, __fmaf_rn(__uint2float_rn(vh >> 8), S.B23, S.nb1));
+        g = fmaxf(fminf(g, 1.0f), 0.0f);
+    } else {
+        const float y = __uint_as_float(((vh >> 8) & 0x7FFFFFu) | 0x3F800000u);
+        const float nc = (static_cast<int32_t>(vh) < 0) ? -1.0f : -2.0f;
+        g = __fadd_rn(par, __fmul_rn(__fadd_rn(y, nc), S.B));
+        g = (g != g) ? 1.0f : fmaxf(fminf(g, 1.0f), 0.0f);
+    }
+    return g;
+}
+
 // One candidate: genes in registers, score in the reference's op order
 // (src/screen.zig:97-112):
 //   lane l:  acc_l = w0 + wl_l*g_l;  sum_l = sum_{i=l..15} Wq[i][l]*(g_l*g_i)
@@ -189,6 +236,8 @@ template <bool kFastDelta, bool kKeepGenes, bool kExact = true, class Model = De
 __device__ __forceinline__ float synth_score(const Model &M, const SynthConst &C,
                                              const float *__restrict__ el, uint64_t seed_t,
                                              uint64_t p, const CandHead &h, float *genes) {
+    // next_gene's synthesis written out: through the helper the compiler
+    // allocates this hot loop's registers differently (0.3% slower, measured)
     const uint64_t s0 = seed_t + (p + 1) * kGolden;
     const uint32_t ra = h.imm ? C.ne : h.ea;
     const uint32_t rb = h.imm ? C.ne : h.eb;
@@ -265,36 +314,13 @@ template <bool kFastDelta, bool kKeepGenes>
 __device__ __forceinline__ float synth_full(const FullModel &M, const SynthConst &C,
                                             const float *__restrict__ el, uint64_t seed_t, uint64_t p,
                                             const CandHead &h, float *genes) {
-    const uint64_t s0 = seed_t + (p + 1) * kGolden;
-    const uint32_t ra = h.imm ? C.ne : h.ea;
-    const uint32_t rb = h.imm ? C.ne : h.eb;
-    const float *pa = el + ra * kNtot;
-    const float *pb = el + rb * kNtot;
-    const float B = h.imm ? 0.5f : C.sigma;
-    const float nb1 = h.imm ? -0.5f : C.nsig1;
-    const float B23 = h.imm ? 0x1p-24f : C.sigma23;
-    const uint64_t step = h.imm ? kGolden : 2 * kGolden;
-    uint64_t su = s0 + (h.imm ? 3ull : 4ull) * kGolden;
+    GeneSource S = gene_source(C, el, seed_t, p, h);
 
     float G[kNtot];
     float R = M.w0;
 #pragma unroll
     for (int k = 0; k < kNtot; ++k) {
-        const uint32_t bw = draw_bitword(su - kGolden);
-        const uint32_t vh = draw_vh(su);
-        su += step;
-        const float *src = (static_cast<int32_t>(bw) < 0) ? pb : pa;
-        const float par = src[k];
-        float g;
-        if (kFastDelta) {
-            g = __fadd_rn(par, __fmaf_rn(__uint2float_rn(vh >> 8), B23, nb1));
-            g = fmaxf(fminf(g, 1.0f), 0.0f);
-        } else {
-            const float y = __uint_as_float(((vh >> 8) & 0x7FFFFFu) | 0x3F800000u);
-            const float nc = (static_cast<int32_t>(vh) < 0) ? -1.0f : -2.0f;
-            g = __fadd_rn(par, __fmul_rn(__fadd_rn(y, nc), B));
-            g = (g != g) ? 1.0f : fmaxf(fminf(g, 1.0f), 0.0f);
-        }
+        float g = next_gene<kFastDelta>(S, k);
         g = (static_cast<uint32_t>(k) == h.jidx) ? h.jval : g;
         if (kKeepGenes) genes[k] = g;
         G[k] = g;

@@ -184,34 +184,11 @@ template <bool kFastDelta, bool kFp16>
 __device__ __forceinline__ void synth_tc(const TcModel &T, const SynthConst &C, const float *__restrict__ el,
                                          uint64_t seed_t, uint64_t p, const CandHead &h, float &R, float (&x)[16],
                                          uint32_t (&pk)[8]) {
-    const uint64_t s0 = seed_t + (p + 1) * kGolden;
-    const uint32_t ra = h.imm ? C.ne : h.ea;
-    const uint32_t rb = h.imm ? C.ne : h.eb;
-    const float *pa = el + ra * kNtot;
-    const float *pb = el + rb * kNtot;
-    const float B = h.imm ? 0.5f : C.sigma;
-    const float nb1 = h.imm ? -0.5f : C.nsig1;
-    const float B23 = h.imm ? 0x1p-24f : C.sigma23;
-    const uint64_t step = h.imm ? kGolden : 2 * kGolden;
-    uint64_t su = s0 + (h.imm ? 3ull : 4ull) * kGolden;
+    GeneSource S = gene_source(C, el, seed_t, p, h);
     R = T.c;
 #pragma unroll
     for (int k = 0; k < kNtot; ++k) {
-        const uint32_t bw = draw_bitword(su - kGolden);
-        const uint32_t vh = draw_vh(su);
-        su += step;
-        const float *src = (static_cast<int32_t>(bw) < 0) ? pb : pa;
-        const float par = src[k];
-        float g;
-        if (kFastDelta) {
-            g = __fadd_rn(par, __fmaf_rn(__uint2float_rn(vh >> 8), B23, nb1));
-            g = fmaxf(fminf(g, 1.0f), 0.0f);
-        } else {
-            const float y = __uint_as_float(((vh >> 8) & 0x7FFFFFu) | 0x3F800000u);
-            const float nc = (static_cast<int32_t>(vh) < 0) ? -1.0f : -2.0f;
-            g = __fadd_rn(par, __fmul_rn(__fadd_rn(y, nc), B));
-            g = (g != g) ? 1.0f : fmaxf(fminf(g, 1.0f), 0.0f);
-        }
+        const float g = next_gene<kFastDelta>(S, k);
         // no jump here: the caller lowers the threshold by JumpBound::c[h.jidx]
         R = __fmaf_rn(T.lin[k], g, R);
         if (k < 16) x[k] = kFp16 ? __fmaf_rn(g, 2.0f, -1.0f) : g;
