@@ -163,3 +163,15 @@ def test_gpu_full_screen_refuses_precision_flags(csx):
     with pytest.raises(CsxError) as e:
         screen.screen(cfg, screen.ModelFull.from_compact(_weights(1)), wl.seeded_elites(8))
     assert e.value.status == _lib.ERR_BAD_ARGS
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("sigma", [1e-31, 2e-40, 3e38, float("inf"), float("nan"), -0.25])
+def test_gpu_full_screen_sigma_edge_cases(csx, orc, sigma):
+    """Mutation widths outside the fast delta form's range (the exact two-op
+    form, NaN genes clamped to 1) on the full surface."""
+    if not has_gpu():
+        pytest.skip("no CUDA device")
+    from codec_arena_gb300 import workloads as wl
+
+    _check_screen(orc, 20_000, 30, 4, 4, _weights(31, 0.3), wl.seeded_elites(64), sigma=sigma)

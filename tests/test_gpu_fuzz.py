@@ -73,3 +73,20 @@ def test_random_batch_matches_single_screens(b):
         want, wn = screen.screen(c, m, e)
         assert n == wn
         assert surv.tobytes() == want.tobytes()
+
+
+@pytest.mark.parametrize("i", range(12))
+def test_random_config_full_surface_matches_oracle(orc, i):
+    """The same random configurations screened on the full 29-gene surface
+    (465 random coefficients) against the oracle's full-surface screen."""
+    from codec_arena_gb300 import screen
+
+    lam, T, keep, _, sigma, jump, imm, el, seed = _config(100 + i)
+    rng = np.random.default_rng(2000 + i)
+    w = (rng.normal(0, 1, 465) * float(rng.choice([0.1, 1.0, 30.0]))).astype(np.float32)
+    cfg = screen.Cfg(lam, keep, seed, threads=T, sigma=sigma, jump_p=jump, imm_p=imm)
+    got, n = screen.screen(cfg, screen.ModelFull.from_compact(w), el)
+    oc = orc.cfg(lam, keep, seed, threads=T, sigma=sigma, jump_p=jump, imm_p=imm)
+    want, wn = orc.screen(oc, orc.model_full_from_compact(w), el, cpu_threads=os.cpu_count() or 4)
+    assert n == wn == lam
+    assert_same_modulo_ties(got, want)
