@@ -152,9 +152,13 @@ __device__ __forceinline__ CandHead cand_head(const SynthConst &C, uint64_t seed
     h.imm = (draw_vh(s0 + 2 * kGolden) >> 8) < C.imm_thr;
     const uint64_t sj = s0 + (h.imm ? 32ull : 61ull) * kGolden;  // draw p+3+29 / p+3+58
     const bool jump = (draw_vh(sj) >> 8) < C.jump_thr;
-    const uint32_t idx = draw_hi(sj + kGolden) % 29u;             // index drawn first
-    h.jval = static_cast<float>(draw_vh(sj + 2 * kGolden) >> 8) * (1.0f / 16777216.0f);
-    h.jidx = jump ? idx : kNoJump;
+    // the index (drawn first) and value only for the 2% that jump
+    h.jidx = kNoJump;
+    h.jval = 0.0f;
+    if (jump) {
+        h.jidx = draw_hi(sj + kGolden) % 29u;
+        h.jval = static_cast<float>(draw_vh(sj + 2 * kGolden) >> 8) * (1.0f / 16777216.0f);
+    }
     h.len = (h.imm ? 33u : 62u) + (jump ? 2u : 0u);
     return h;
 }
