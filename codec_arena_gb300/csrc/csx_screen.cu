@@ -279,12 +279,14 @@ int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int
         if (rc) return rc;
     }
 
-    // item size D: about 64 items per screen thread (measured: smaller items
-    // shorten the tail of the persistent grid more than their reads cost;
-    // 256 candidates at 2.65e9 beat 512 by 0.5% and 128 by 0.1%)
+    // item size D: about 64 items per thread of a three-CTA-per-SM grid, set
+    // by the GPU's size rather than the kernel's grid (measured: smaller items
+    // shorten the tail of the persistent grid more than their reads cost; at
+    // 2.65e9, 256 candidates beat 512 by 0.5% with three CTAs per SM and by
+    // 0.25% with the filter kernel's two)
     uint64_t d = item_cands ? item_cands : env_u64("CSX_ITEM_CANDS", 0);
     if (d == 0) {
-        const uint64_t target = 64ull * static_cast<uint64_t>(pl->grid) * kThreads;
+        const uint64_t target = 64ull * 3 * static_cast<uint64_t>(cx.num_sms) * kThreads;
         d = std::max<uint64_t>(1, lam_range / target);
         d = std::min<uint64_t>(16384, std::max<uint64_t>(64, d));
     }

@@ -214,8 +214,10 @@ __global__ void __launch_bounds__(kThreads, 3) screen_kernel(const __grid_consta
 // the other 31 of its warp wait. The buffer fills only from the queue, and
 // every fill is sorted at once, so it always has room (queue + one held entry
 // per thread <= 768 <= sort_n - kpad).
+// Two CTAs per SM with up to 128 registers: 1% faster than three at 80
+// (measured; the other screen kernels are faster at three).
 template <bool kFastDelta>
-__global__ void __launch_bounds__(kThreads, 3) screen_q_kernel(const __grid_constant__ ScreenArgs A) {
+__global__ void __launch_bounds__(kThreads, 2) screen_q_kernel(const __grid_constant__ ScreenArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Entry *E = reinterpret_cast<Entry *>(smem_raw);
     float *el = reinterpret_cast<float *>(E + A.sort_n);
