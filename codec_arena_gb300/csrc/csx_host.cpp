@@ -182,7 +182,10 @@ int csx_model_from_compact(const float *w, int n, csx_model *m) {
 }
 
 // loadModel body: src/screen.zig:118-126.
-int csx_model_parse(const char *txt, size_t len, float *w, int cap, int *n_out) {
+namespace {
+// loadModel's text body; allow_full also takes the full surface's 465
+// coefficients (the `arena screen` verb of this implementation).
+int model_parse(const char *txt, size_t len, float *w, int cap, int *n_out, bool allow_full) {
     if (!txt || !w || !n_out) return CSX_ERR_BAD_ARGS;
     const char *ws = " \t\r\n";
     size_t i = 0;
@@ -200,7 +203,8 @@ int csx_model_parse(const char *txt, size_t len, float *w, int cap, int *n_out) 
     if (!next_tok(&t)) return CSX_ERR_BAD_MODEL;
     uint64_t n64;
     if (!parse_uint(t.p, t.n, UINT64_MAX, &n64)) return CSX_ERR_PARSE;
-    if (n64 > 1000 || !valid_n(static_cast<int>(n64))) return CSX_ERR_BAD_MODEL;
+    if (n64 > 1000 || !(valid_n(static_cast<int>(n64)) || (allow_full && n64 == CSX_FULL_NF)))
+        return CSX_ERR_BAD_MODEL;
     const int n = static_cast<int>(n64);
     if (n > cap) return CSX_ERR_BAD_ARGS;
     for (int k = 0; k < n; ++k) {
@@ -209,6 +213,11 @@ int csx_model_parse(const char *txt, size_t len, float *w, int cap, int *n_out) 
     }
     *n_out = n;
     return CSX_OK;
+}
+}  // namespace
+
+int csx_model_parse(const char *txt, size_t len, float *w, int cap, int *n_out) {
+    return model_parse(txt, len, w, cap, n_out, false);
 }
 
 // parseLine: src/genome.zig:116-188.
@@ -380,12 +389,16 @@ int csx_screen_cli(int argc, const char *const *argv) {
     }
     std::string txt;
     if (!read_file(model_path.c_str(), 1u << 20, &txt)) return fail(CSX_ERR_IO, model_path.c_str());
-    float w[166];
+    // a model file of 465 coefficients is the full 29-gene surface (an
+    // extension: the reference's loadModel refuses it)
+    std::vector<float> w(CSX_FULL_NF);
     int n = 0;
-    int st = csx_model_parse(txt.data(), txt.size(), w, 166, &n);
+    int st = model_parse(txt.data(), txt.size(), w.data(), CSX_FULL_NF, &n, true);
     if (st) return fail(st, model_path.c_str());
-    csx_model model;
-    st = csx_model_from_compact(w, n, &model);
+    const bool full = n == CSX_FULL_NF;
+    csx_model model{};
+    csx_model_full model_full{};
+    st = full ? csx_model_full_from_compact(w.data(), n, &model_full) : csx_model_from_compact(w.data(), n, &model);
     if (st) return fail(st, model_path.c_str());
     if (!read_file(elites_path.c_str(), 1u << 22, &txt)) return fail(CSX_ERR_IO, elites_path.c_str());
     int ne = 0;
@@ -396,7 +409,8 @@ int csx_screen_cli(int argc, const char *const *argv) {
     const uint64_t cap = cfg.keep < cfg.lambda ? cfg.keep : cfg.lambda;
     std::vector<csx_survivor> surv(static_cast<size_t>(cap > 0 ? cap : 1));
     uint64_t n_out = 0, screened = 0;
-    st = csx_screen(&cfg, &model, elites.data(), ne, surv.data(), cap, &n_out, &screened);
+    st = full ? csx_screen_full(&cfg, &model_full, elites.data(), ne, surv.data(), cap, &n_out, &screened)
+              : csx_screen(&cfg, &model, elites.data(), ne, surv.data(), cap, &n_out, &screened);
     if (st) return fail(st, nullptr);
     FILE *f = std::fopen(out_path.c_str(), "wb");
     if (!f) return fail(CSX_ERR_IO, out_path.c_str());

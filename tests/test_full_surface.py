@@ -175,3 +175,28 @@ def test_gpu_full_screen_sigma_edge_cases(csx, orc, sigma):
     from codec_arena_gb300 import workloads as wl
 
     _check_screen(orc, 20_000, 30, 4, 4, _weights(31, 0.3), wl.seeded_elites(64), sigma=sigma)
+
+
+@pytest.mark.gpu
+def test_gpu_cli_takes_a_full_surface_model(csx, tmp_path):
+    """`arena screen --model F` with a 465-coefficient file (as
+    brain.save_weights writes it) screens on the full surface; the promoted
+    file equals the in-process screen's survivors."""
+    if not has_gpu():
+        pytest.skip("no CUDA device")
+    from codec_arena_gb300 import brain, cli, genome, screen, workloads as wl
+
+    w = _weights(44, 0.3).astype(np.float64)
+    model_path = tmp_path / "surrogate.txt"
+    brain.save_weights(str(model_path), list(w))
+    el = wl.seeded_elites(24)
+    el_path = tmp_path / "elites.txt"
+    el_path.write_text("".join(genome.format_line(r) + "\n" for r in el))
+    out, cnt = tmp_path / "promoted.txt", tmp_path / "screens.txt"
+    rc = cli.main(["screen", "--model", str(model_path), "--elites", str(el_path), "--out", str(out),
+                   "--count-out", str(cnt), "--lambda", "150000", "--keep", "40", "--seed", "77"])
+    assert rc == 0 and cnt.read_text() == "150000\n"
+    w32 = np.array([np.float32(f"{x:.8e}") for x in w], dtype=np.float32)  # the file's text, as parsed
+    cfg = screen.Cfg(150_000, 40, 77)
+    want, _ = screen.screen(cfg, screen.ModelFull.from_compact(w32), genome.load_elites_text(el_path.read_text()))
+    assert out.read_text() == "".join(screen.format_survivor(r) for r in want)
