@@ -373,15 +373,6 @@ __device__ __forceinline__ float score_genes_exact(const DevModel &M, const floa
     return __fadd_rn(r, R);
 }
 
-// Candidate-start walk: the start of the candidate after the one at p (the
-// immigrant test, then the jump test at the position it implies).
-__device__ __forceinline__ uint64_t walk_step2(const SynthConst &C, uint64_t seed_t, uint64_t p) {
-    const uint64_t s0 = seed_t + (p + 1) * kGolden;
-    const bool imm = (draw_vh(s0 + 2 * kGolden) >> 8) < C.imm_thr;
-    const bool jump = (draw_vh(s0 + (imm ? 32ull : 61ull) * kGolden) >> 8) < C.jump_thr;
-    return p + (imm ? 33u : 62u) + (jump ? 2u : 0u);
-}
-
 // Length of the candidate whose start draw has state st = seed_t + (p + 1) *
 // kGolden: the immigrant test and the crossover candidate's jump test hashed
 // side by side, the immigrant's own jump test only when it is one.
