@@ -46,10 +46,10 @@ struct DevModel {
     float wq[kNq];  // (i, j <= i) at i*(i+1)/2 + j  ==  Model.w_quad[i*16 + j]
 };
 
-// Bound on how far a jump can move the real score: with every gene in [0, 1],
-// setting gene j to another value in [0, 1] changes the surface by at most
-// c[j] = |w_lin[j]| + sum_i |Wq[i][j]| + sum_i |Wq[j][i]| (i != j) + |Wq[j][j]|
-// (rounded up). c[kNoJump] = 0, as are the unused entries.
+// Bound on how far a jump can raise the real score: with every gene in
+// [0, 1], setting gene j to another value in [0, 1] raises the surface by at
+// most c[j] (host: jump_bound, from the signs of w_lin[j] and gene j's
+// quadratic terms; rounded up). c[kNoJump] = 0, as are the unused entries.
 struct JumpBound {
     float c[32];
 };

@@ -210,17 +210,30 @@ float filter_bound(const csx_model &m) {
     return std::nextafter(static_cast<float>(e), INFINITY);
 }
 
-// JumpBound of a model whose filter_bound is nonzero (finite weights): the
-// change of the real surface when gene j moves within [0, 1], computed in
-// double and rounded up with a 2^-20 relative margin.
+// JumpBound of a model whose filter_bound is nonzero (finite weights): an
+// upper bound on how far the real surface can rise when gene j moves within
+// [0, 1] (only a rise can lift a candidate over the threshold). With δ = v -
+// u the move and the other genes in [0, 1], the change is
+// δ (w_j + Σ_{i≠j} Q_ij g_i) + Q_jj (v² - u²): at most max(0, a_hi) +
+// max(0, Q_jj) for δ >= 0 and max(0, -a_lo) + max(0, -Q_jj) for δ < 0, where
+// a_hi / a_lo add the positive / negative Q_ij to w_j. Computed in double and
+// rounded up with a 2^-20 relative margin.
 void jump_bound(const csx_model &m, JumpBound *jb) {
     for (int j = 0; j < 32; ++j) jb->c[j] = 0.0f;
     for (int j = 0; j < kNtot; ++j) {
-        double c = std::fabs(static_cast<double>(m.w_lin[j]));
-        if (j < 16)
-            for (int i = 0; i < 16; ++i)  // row j (i <= j) and column j (i > j) of the triangle
-                c += std::fabs(static_cast<double>(i <= j ? m.w_quad[j * 16 + i] : m.w_quad[i * 16 + j]));
-        c *= 1.0 + std::ldexp(1.0, -20);
+        const double w = static_cast<double>(m.w_lin[j]);
+        double a_hi = w, a_lo = w, qjj = 0.0;
+        if (j < 16) {
+            for (int i = 0; i < 16; ++i) {  // row j (i <= j) and column j (i > j) of the triangle
+                const double q = static_cast<double>(i <= j ? m.w_quad[j * 16 + i] : m.w_quad[i * 16 + j]);
+                if (i == j) qjj = q;
+                else if (q > 0.0) a_hi += q;
+                else a_lo += q;
+            }
+        }
+        const double up = std::max(0.0, a_hi) + std::max(0.0, qjj);
+        const double down = std::max(0.0, -a_lo) + std::max(0.0, -qjj);
+        const double c = std::max(up, down) * (1.0 + std::ldexp(1.0, -20));
         jb->c[j] = c > 0.0 ? std::nextafter(static_cast<float>(c), INFINITY) : 0.0f;
     }
 }
