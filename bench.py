@@ -58,7 +58,7 @@ LANE_OPS_PER_CAND = 1760.0
 DRAWS_PER_CAND = 61.75
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
@@ -76,7 +76,7 @@ def parse():
     ap.add_argument("--islands", type=int, default=20)
     ap.add_argument("--islands-scale", type=float, default=1.0,
                     help="scale every island budget (small cases for profiling)")
-    return ap.parse_args()
+    return ap.parse_args(argv)
 
 
 def dist_env():
@@ -209,7 +209,7 @@ def run_reference(args):
         times.append(time.perf_counter() - t0)
     tot = sum(times)
     v = lam * steps / tot
-    line = {"impl": "reference", "metric": "candidates/sec (screen generation, 1 GB300 host)",
+    line = {"impl": "reference", "metric": METRIC,
             "value": v, "unit": "candidates/s", "n_gpus": world, "steps": steps, "warmup": warm,
             "ms_per_step": 1000 * tot / steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": v / PUBLISHED_CAND_S, "vs_baseline_source": PUBLISHED_SOURCE,

@@ -19,4 +19,10 @@ def test_reference_arm_line():
               "config", "cpu_baseline", "e2e"):
         assert k in line, k
     assert line["value"] > 0 and line["e2e"]["h2d_bytes_per_step"] == 0
+    # the same metric, unit and direction as our arm's line
+    sys.path.insert(0, ROOT)
+    import bench
+
+    assert (line["metric"], line["unit"], line["higher_is_better"]) == (bench.METRIC, "candidates/s", True)
+    assert line["config"] == bench.workload_config(bench.parse([]), 1)
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["value"] == line["value"]
