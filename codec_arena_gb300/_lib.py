@@ -166,6 +166,8 @@ SIGNATURES.update({
     "csx_model_full_from_compact": (_int, [ctypes.POINTER(_f32), _int, ctypes.POINTER(CsxModelFull)]),
     "csx_screen_full": (_int, [ctypes.POINTER(CsxCfg), ctypes.POINTER(CsxModelFull), _vp, _int, _vp, _u64,
                                ctypes.POINTER(_u64), ctypes.POINTER(_u64)]),
+    "csx_screen_full_range": (_int, [ctypes.POINTER(CsxCfg), ctypes.POINTER(CsxModelFull), _vp, _int, _u64, _u64,
+                                     _vp, _u64, ctypes.POINTER(_u64), ctypes.POINTER(_u64)]),
     "csx_screen_full_device": (_int, [ctypes.POINTER(CsxCfg), ctypes.POINTER(CsxModelFull), _vp, _int, _vp,
                                       _u64, _vp, _vp]),
     "csx_score_full": (_int, [ctypes.POINTER(CsxModelFull), _vp, _i64, _int, _vp, _vp]),

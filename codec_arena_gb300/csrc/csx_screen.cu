@@ -684,6 +684,17 @@ int csx_screen_full(const csx_cfg *cfg, const csx_model_full *model, const csx_g
     return screen_host(cfg, &kZeroModel, elites, n_elites, 0, 0, out, out_cap, n_out, screened, model);
 }
 
+int csx_screen_full_range(const csx_cfg *cfg, const csx_model_full *model, const csx_genome *elites,
+                          int n_elites, uint64_t t_begin, uint64_t t_end, csx_survivor *out, uint64_t out_cap,
+                          uint64_t *n_out, uint64_t *screened) {
+    if (!model || t_end <= t_begin) {
+        if (n_out) *n_out = 0;
+        if (screened) *screened = 0;
+        return CSX_ERR_BAD_ARGS;
+    }
+    return screen_host(cfg, &kZeroModel, elites, n_elites, t_begin, t_end, out, out_cap, n_out, screened, model);
+}
+
 int csx_screen_range(const csx_cfg *cfg, const csx_model *model, const csx_genome *elites, int n_elites,
                      uint64_t t_begin, uint64_t t_end, csx_survivor *out, uint64_t out_cap, uint64_t *n_out,
                      uint64_t *screened) {

@@ -144,12 +144,14 @@ def screen(cfg: Cfg, model: Model, elites, streams: Optional[Tuple[int, int]] = 
     n_out = ctypes.c_uint64(0)
     screened = ctypes.c_uint64(0)
     c = cfg.c()
-    if isinstance(model, ModelFull):
-        if streams is not None:
-            raise ValueError("the full surface screens whole generations")
+    if isinstance(model, ModelFull) and streams is None:
         check(lib().csx_screen_full(ctypes.byref(c), ctypes.byref(model.c), e.ctypes.data, int(e.shape[0]),
                                     out.ctypes.data, keep_n, ctypes.byref(n_out), ctypes.byref(screened)),
               "screen_full")
+    elif isinstance(model, ModelFull):
+        check(lib().csx_screen_full_range(ctypes.byref(c), ctypes.byref(model.c), e.ctypes.data, int(e.shape[0]),
+                                          int(streams[0]), int(streams[1]), out.ctypes.data, keep_n,
+                                          ctypes.byref(n_out), ctypes.byref(screened)), "screen_full_range")
     elif streams is None:
         check(lib().csx_screen(ctypes.byref(c), ctypes.byref(model.c), e.ctypes.data, int(e.shape[0]),
                                out.ctypes.data, keep_n, ctypes.byref(n_out), ctypes.byref(screened)),

@@ -300,6 +300,10 @@ int csx_model_full_from_compact(const float *w, int n, csx_model_full *out);
  * surface. The precision-form flags are refused (CSX_ERR_BAD_ARGS). */
 int csx_screen_full(const csx_cfg *cfg, const csx_model_full *model, const csx_genome *elites, int n_elites,
                     csx_survivor *out, uint64_t out_cap, uint64_t *n_out, uint64_t *screened);
+/* csx_screen_range on the full surface: the RNG streams [t_begin, t_end). */
+int csx_screen_full_range(const csx_cfg *cfg, const csx_model_full *model, const csx_genome *elites,
+                          int n_elites, uint64_t t_begin, uint64_t t_end, csx_survivor *out, uint64_t out_cap,
+                          uint64_t *n_out, uint64_t *screened);
 int csx_screen_full_device(const csx_cfg *cfg, const csx_model_full *model, const csx_genome *d_elites,
                            int n_elites, csx_survivor *d_out, uint64_t out_cap, uint64_t *d_result,
                            void *cuda_stream);

@@ -200,3 +200,21 @@ def test_gpu_cli_takes_a_full_surface_model(csx, tmp_path):
     cfg = screen.Cfg(150_000, 40, 77)
     want, _ = screen.screen(cfg, screen.ModelFull.from_compact(w32), genome.load_elites_text(el_path.read_text()))
     assert out.read_text() == "".join(screen.format_survivor(r) for r in want)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("lam,T,parts", [(8_000_000, 4, [(0, 1), (1, 3), (3, 4)]), (300_000, 7, [(0, 5), (5, 7)])])
+def test_gpu_full_stream_ranges_merge_to_the_generation(csx, lam, T, parts):
+    """csx_screen_full_range on a partition of the streams, merged in the
+    reference's order, equals the whole full-surface generation bit for bit."""
+    if not has_gpu():
+        pytest.skip("no CUDA device")
+    from codec_arena_gb300 import parallel, screen, workloads as wl
+
+    el = wl.seeded_elites(64)
+    m = screen.ModelFull.from_compact(_weights(55, 0.3))
+    cfg = screen.Cfg(lam, 96, 13, threads=T)
+    whole, n = screen.screen(cfg, m, el)
+    pieces = [screen.screen(cfg, m, el, streams=p) for p in parts]
+    assert sum(p[1] for p in pieces) == n == lam
+    assert parallel.merge_survivors([p[0] for p in pieces], 96).tobytes() == whole.tobytes()
