@@ -353,17 +353,6 @@ BatchFn batch_fn(bool fast_delta, bool filter) {
     return filter ? screen_batch_kernel<false, true> : screen_batch_kernel<false, false>;
 }
 
-SynthConst make_synth(const csx_cfg &cfg, int ne) {
-    SynthConst sc;
-    sc.ne = static_cast<uint32_t>(ne);
-    sc.ne_magic = ~0ull / static_cast<uint64_t>(ne) + 1;
-    sc.imm_thr = unit_threshold(cfg.imm_p);
-    sc.jump_thr = unit_threshold(cfg.jump_p);
-    sc.sigma = cfg.sigma;
-    sc.nsig1 = -cfg.sigma;
-    sc.sigma23 = cfg.sigma * 0x1p-23f;
-    return sc;
-}
 
 RowModel make_row_model(const DevModel &m) {
     RowModel r{};
@@ -377,15 +366,6 @@ RowModel make_row_model(const DevModel &m) {
     return r;
 }
 
-DevModel make_dev_model(const csx_model &model) {
-    DevModel m;
-    m.w0 = model.w0;
-    m.w16 = 16.0f * model.w0;
-    for (int k = 0; k < kNtot; ++k) m.wlin[k] = model.w_lin[k];
-    for (int i = 0; i < 16; ++i)
-        for (int j = 0; j <= i; ++j) m.wq[tri(i, j)] = model.w_quad[i * 16 + j];
-    return m;
-}
 
 struct IslandBufs {
     const csx_genome *genomes = nullptr;
@@ -578,26 +558,8 @@ int batch_enqueue(Context &cx, const BatchLayout &L, cudaStream_t st, bool captu
         ++nk;
         if (L.cfg[i].lambda > 0) {
             const SynthConst sc = make_synth(L.cfg[i], ne);
-            if (pl.short_path) {
-                stream_items_kernel<<<unit_blocks(g.nT, 256), 256, 0, a>>>(g, b.items, b.ctrl);
-                CSX_CUDA(cudaGetLastError());
-                ++nk;
-            } else {
-                walk_kernel<<<unit_blocks(g.n_seg, 128), 128, 0, a>>>(sc, g, b.recs, b.ck, b.ctrl);
-                CSX_CUDA(cudaGetLastError());
-                link_kernel<<<unit_blocks(g.n_seg * 32, 128), 128, 0, a>>>(sc, g, b.recs, b.ck, b.ctrl);
-                CSX_CUDA(cudaGetLastError());
-                if (g.C >= 64)
-                    assemble_block_kernel<<<static_cast<unsigned>(g.nT), kAsmThreads, 0, a>>>(g, b.recs, b.so, b.ctrl);
-                else
-                    assemble_kernel<<<unit_blocks(g.nT, 128), 128, 0, a>>>(g, b.recs, b.so, b.ctrl);
-                CSX_CUDA(cudaGetLastError());
-                scan_kernel<<<1, 1024, 0, a>>>(b.so, g.n_seg, b.off, b.ctrl, pl.items_cap);
-                CSX_CUDA(cudaGetLastError());
-                emit_kernel<<<unit_blocks(g.n_seg, 128), 128, 0, a>>>(g, b.so, b.off, b.ck, b.items, b.ctrl);
-                CSX_CUDA(cudaGetLastError());
-                nk += 5;
-            }
+            const int rc = enqueue_items(sc, pl, b.recs, b.ck, b.so, b.off, b.items, b.ctrl, a, &nk);
+            if (rc) return rc;
         }
         CSX_CUDA(cudaEventRecord(cx.ev_join[i], a));
         CSX_CUDA(cudaStreamWaitEvent(st, cx.ev_join[i], 0));

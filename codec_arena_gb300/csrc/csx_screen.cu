@@ -329,6 +329,97 @@ int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int
 
 int unit_blocks(uint64_t n, int threads) { return static_cast<int>((n + threads - 1) / threads); }
 
+SynthConst make_synth(const csx_cfg &cfg, int ne) {
+    SynthConst sc;
+    sc.ne = static_cast<uint32_t>(ne);
+    sc.ne_magic = ~0ull / static_cast<uint64_t>(ne) + 1;
+    sc.imm_thr = unit_threshold(cfg.imm_p);
+    sc.jump_thr = unit_threshold(cfg.jump_p);
+    sc.sigma = cfg.sigma;
+    sc.nsig1 = -cfg.sigma;
+    sc.sigma23 = cfg.sigma * 0x1p-23f;
+    return sc;
+}
+
+DevModel make_dev_model(const csx_model &model) {
+    DevModel m;
+    m.w0 = model.w0;
+    m.w16 = 16.0f * model.w0;
+    for (int k = 0; k < kNtot; ++k) m.wlin[k] = model.w_lin[k];
+    for (int i = 0; i < 16; ++i)
+        for (int j = 0; j <= i; ++j) m.wq[tri(i, j)] = model.w_quad[i * 16 + j];
+    return m;
+}
+
+// The item-building stages on `st` (walk, link, assembly, scan, emit), or one
+// item per stream when every stream fits in one item. recs / ck / so / off
+// are unused on the short path.
+int enqueue_items(const SynthConst &sc, const Plan &pl, SegRec *recs, uint64_t *ck, SegOut *so, uint32_t *off,
+                  Item *items, Ctrl *ctrl, cudaStream_t st, uint32_t *launches) {
+    const StreamGeom &g = pl.g;
+    if (pl.short_path) {
+        stream_items_kernel<<<unit_blocks(g.nT, 256), 256, 0, st>>>(g, items, ctrl);
+        CSX_CUDA(cudaGetLastError());
+        ++*launches;
+        return CSX_OK;
+    }
+    walk_kernel<<<unit_blocks(g.n_seg, 128), 128, 0, st>>>(sc, g, recs, ck, ctrl);
+    CSX_CUDA(cudaGetLastError());
+    link_kernel<<<unit_blocks(g.n_seg * 32, 128), 128, 0, st>>>(sc, g, recs, ck, ctrl);
+    CSX_CUDA(cudaGetLastError());
+    if (g.C >= 64)
+        assemble_block_kernel<<<static_cast<unsigned>(g.nT), kAsmThreads, 0, st>>>(g, recs, so, ctrl);
+    else
+        assemble_kernel<<<unit_blocks(g.nT, 128), 128, 0, st>>>(g, recs, so, ctrl);
+    CSX_CUDA(cudaGetLastError());
+    scan_kernel<<<1, 1024, 0, st>>>(so, g.n_seg, off, ctrl, pl.items_cap);
+    CSX_CUDA(cudaGetLastError());
+    emit_kernel<<<unit_blocks(g.n_seg, 128), 128, 0, st>>>(g, so, off, ck, items, ctrl);
+    CSX_CUDA(cudaGetLastError());
+    *launches += 5;
+    return CSX_OK;
+}
+
+// The screen's arguments for a plan (the reference surface's model slot set).
+ScreenArgs screen_args(const csx_cfg &cfg, const csx_model &model, const SynthConst &sc, const Plan &pl,
+                       const float *tab, const Item *items, Ctrl *ctrl, Entry *lists) {
+    ScreenArgs A;
+    A.m = make_dev_model(model);
+    A.sc = sc;
+    A.seed = cfg.seed;
+    A.el = tab;
+    A.items = items;
+    A.ctrl = ctrl;
+    A.lists = lists;
+    A.keep = static_cast<uint32_t>(cfg.keep);
+    A.kpad = pl.kpad;
+    A.sort_n = pl.sort_n;
+    A.buf_cap = pl.buf_cap;
+    A.err = pl.err;
+    A.jb = pl.jb;
+    return A;
+}
+
+// Merge tree of nl CTA lists (kpad entries each) between the two buffers;
+// *fin receives the buffer holding the final list.
+int enqueue_merge(Entry *cur, Entry *nxt, uint32_t nl, uint32_t kpad, cudaStream_t st, Entry **fin,
+                  uint32_t *launches) {
+    const size_t msmem = 2ull * kpad * sizeof(Entry);
+    CSX_CUDA(cudaFuncSetAttribute(merge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(msmem)));
+    uint32_t n = nl;
+    while (n > 1) {
+        const uint32_t m = (n + 1) / 2;
+        merge_kernel<<<m, 256, msmem, st>>>(cur, n, nxt, kpad);
+        CSX_CUDA(cudaGetLastError());
+        ++*launches;
+        std::swap(cur, nxt);
+        n = m;
+    }
+    *fin = cur;
+    return CSX_OK;
+}
+
 // Enqueue the whole pipeline on `st`. Device inputs: genomes (csx_genome x ne).
 int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, const csx_genome *d_genomes,
                    int ne, csx_survivor *d_out, unsigned long long *d_result, cudaStream_t st,
@@ -366,14 +457,7 @@ int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, cons
     CSX_CUDA(mark(0));
     CSX_CUDA(cudaMemsetAsync(ctrl, 0, sizeof(Ctrl), st));
 
-    SynthConst sc;
-    sc.ne = static_cast<uint32_t>(ne);
-    sc.ne_magic = ~0ull / static_cast<uint64_t>(ne) + 1;
-    sc.imm_thr = unit_threshold(cfg.imm_p);
-    sc.jump_thr = unit_threshold(cfg.jump_p);
-    sc.sigma = cfg.sigma;
-    sc.nsig1 = -cfg.sigma;
-    sc.sigma23 = cfg.sigma * 0x1p-23f;
+    const SynthConst sc = make_synth(cfg, ne);
 
     float *tab = static_cast<float *>(cx.tab.p);
     auto *ids = static_cast<unsigned long long *>(cx.ids.p);
@@ -385,50 +469,13 @@ int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, cons
     CSX_CUDA(mark(1));
 
     Item *items = static_cast<Item *>(cx.items.p);
-    if (pl.short_path) {
-        stream_items_kernel<<<unit_blocks(g.nT, 256), 256, 0, st>>>(g, items, ctrl);
-        CSX_CUDA(cudaGetLastError());
-        ++launches;
-    } else {
-        auto *recs = static_cast<SegRec *>(cx.recs.p);
-        auto *ck = static_cast<uint64_t *>(cx.ck.p);
-        auto *so = static_cast<SegOut *>(cx.segout.p);
-        auto *off = static_cast<uint32_t *>(cx.off.p);
-        walk_kernel<<<unit_blocks(g.n_seg, 128), 128, 0, st>>>(sc, g, recs, ck, ctrl);
-        CSX_CUDA(cudaGetLastError());
-        link_kernel<<<unit_blocks(g.n_seg * 32, 128), 128, 0, st>>>(sc, g, recs, ck, ctrl);
-        CSX_CUDA(cudaGetLastError());
-        if (g.C >= 64)
-            assemble_block_kernel<<<static_cast<unsigned>(g.nT), kAsmThreads, 0, st>>>(g, recs, so, ctrl);
-        else
-            assemble_kernel<<<unit_blocks(g.nT, 128), 128, 0, st>>>(g, recs, so, ctrl);
-        CSX_CUDA(cudaGetLastError());
-        scan_kernel<<<1, 1024, 0, st>>>(so, g.n_seg, off, ctrl, pl.items_cap);
-        CSX_CUDA(cudaGetLastError());
-        emit_kernel<<<unit_blocks(g.n_seg, 128), 128, 0, st>>>(g, so, off, ck, items, ctrl);
-        CSX_CUDA(cudaGetLastError());
-        launches += 5;
-    }
+    rc = enqueue_items(sc, pl, static_cast<SegRec *>(cx.recs.p), static_cast<uint64_t *>(cx.ck.p),
+                       static_cast<SegOut *>(cx.segout.p), static_cast<uint32_t *>(cx.off.p), items, ctrl, st,
+                       &launches);
+    if (rc) return rc;
     CSX_CUDA(mark(2));
 
-    ScreenArgs A;
-    A.m.w0 = model.w0;
-    A.m.w16 = 16.0f * model.w0;
-    for (int k = 0; k < kNtot; ++k) A.m.wlin[k] = model.w_lin[k];
-    for (int i = 0; i < 16; ++i)
-        for (int j = 0; j <= i; ++j) A.m.wq[tri(i, j)] = model.w_quad[i * 16 + j];
-    A.sc = sc;
-    A.seed = cfg.seed;
-    A.el = tab;
-    A.items = items;
-    A.ctrl = ctrl;
-    A.lists = static_cast<Entry *>(cx.lists_a.p);
-    A.keep = static_cast<uint32_t>(cfg.keep);
-    A.kpad = pl.kpad;
-    A.sort_n = pl.sort_n;
-    A.buf_cap = pl.buf_cap;
-    A.err = pl.err;
-    A.jb = pl.jb;
+    const ScreenArgs A = screen_args(cfg, model, sc, pl, tab, items, ctrl, static_cast<Entry *>(cx.lists_a.p));
     if (pl.tc) {
         TcScreenArgs P;
         P.A = A;
@@ -450,20 +497,10 @@ int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, cons
     ++launches;
     CSX_CUDA(mark(3));
 
-    // merge tree
-    const size_t msmem = 2ull * pl.kpad * sizeof(Entry);
-    CSX_CUDA(cudaFuncSetAttribute(merge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  static_cast<int>(msmem)));
-    Entry *cur = static_cast<Entry *>(cx.lists_a.p), *nxt = static_cast<Entry *>(cx.lists_b.p);
-    uint32_t n = nl;
-    while (n > 1) {
-        const uint32_t m = (n + 1) / 2;
-        merge_kernel<<<m, 256, msmem, st>>>(cur, n, nxt, pl.kpad);
-        CSX_CUDA(cudaGetLastError());
-        ++launches;
-        std::swap(cur, nxt);
-        n = m;
-    }
+    Entry *cur = nullptr;
+    rc = enqueue_merge(static_cast<Entry *>(cx.lists_a.p), static_cast<Entry *>(cx.lists_b.p), nl, pl.kpad, st,
+                       &cur, &launches);
+    if (rc) return rc;
     CSX_CUDA(mark(4));
     if (full) {
         FullScreenArgs F;
@@ -846,67 +883,19 @@ int enqueue_screen_noalloc(const NoAllocDevice &dv, const csx_cfg &cfg, const cs
         return CSX_ERR_LIMIT;
     }
     CSX_CUDA(cudaMemsetAsync(ctrl, 0, sizeof(Ctrl), st));
-    SynthConst sc;
-    sc.ne = static_cast<uint32_t>(ne);
-    sc.ne_magic = ~0ull / static_cast<uint64_t>(ne) + 1;
-    sc.imm_thr = unit_threshold(cfg.imm_p);
-    sc.jump_thr = unit_threshold(cfg.jump_p);
-    sc.sigma = cfg.sigma;
-    sc.nsig1 = -cfg.sigma;
-    sc.sigma23 = cfg.sigma * 0x1p-23f;
+    const SynthConst sc = make_synth(cfg, ne);
+    uint32_t launches = 0;
     prep_elites_kernel<<<unit_blocks(static_cast<uint64_t>(ne + 1) * kNtot, 256), 256, 0, st>>>(
         d_genomes, ne, tab, ids, tribes);
     CSX_CUDA(cudaGetLastError());
-    if (pl.short_path) {
-        stream_items_kernel<<<unit_blocks(g.nT, 256), 256, 0, st>>>(g, items, ctrl);
-        CSX_CUDA(cudaGetLastError());
-    } else {
-        walk_kernel<<<unit_blocks(g.n_seg, 128), 128, 0, st>>>(sc, g, recs, ck, ctrl);
-        CSX_CUDA(cudaGetLastError());
-        link_kernel<<<unit_blocks(g.n_seg * 32, 128), 128, 0, st>>>(sc, g, recs, ck, ctrl);
-        CSX_CUDA(cudaGetLastError());
-        if (g.C >= 64)
-            assemble_block_kernel<<<static_cast<unsigned>(g.nT), kAsmThreads, 0, st>>>(g, recs, so, ctrl);
-        else
-            assemble_kernel<<<unit_blocks(g.nT, 128), 128, 0, st>>>(g, recs, so, ctrl);
-        CSX_CUDA(cudaGetLastError());
-        scan_kernel<<<1, 1024, 0, st>>>(so, g.n_seg, off, ctrl, pl.items_cap);
-        CSX_CUDA(cudaGetLastError());
-        emit_kernel<<<unit_blocks(g.n_seg, 128), 128, 0, st>>>(g, so, off, ck, items, ctrl);
-        CSX_CUDA(cudaGetLastError());
-    }
-    ScreenArgs A;
-    A.m.w0 = model.w0;
-    A.m.w16 = 16.0f * model.w0;
-    for (int k = 0; k < kNtot; ++k) A.m.wlin[k] = model.w_lin[k];
-    for (int i = 0; i < 16; ++i)
-        for (int j = 0; j <= i; ++j) A.m.wq[tri(i, j)] = model.w_quad[i * 16 + j];
-    A.sc = sc;
-    A.seed = cfg.seed;
-    A.el = tab;
-    A.items = items;
-    A.ctrl = ctrl;
-    A.lists = lists_a;
-    A.keep = static_cast<uint32_t>(cfg.keep);
-    A.kpad = pl.kpad;
-    A.sort_n = pl.sort_n;
-    A.buf_cap = pl.buf_cap;
-    A.err = pl.err;
-    A.jb = pl.jb;
+    rc = enqueue_items(sc, pl, recs, ck, so, off, items, ctrl, st, &launches);
+    if (rc) return rc;
+    const ScreenArgs A = screen_args(cfg, model, sc, pl, tab, items, ctrl, lists_a);
     screen_fn(fast, pl.filter)<<<pl.grid, kThreads, pl.smem, st>>>(A);
     CSX_CUDA(cudaGetLastError());
-    const size_t msmem = 2ull * pl.kpad * sizeof(Entry);
-    CSX_CUDA(cudaFuncSetAttribute(merge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  static_cast<int>(msmem)));
-    Entry *cur = lists_a, *nxt = lists_b;
-    uint32_t n = nl;
-    while (n > 1) {
-        const uint32_t m = (n + 1) / 2;
-        merge_kernel<<<m, 256, msmem, st>>>(cur, n, nxt, pl.kpad);
-        CSX_CUDA(cudaGetLastError());
-        std::swap(cur, nxt);
-        n = m;
-    }
+    Entry *cur = nullptr;
+    rc = enqueue_merge(lists_a, lists_b, nl, pl.kpad, st, &cur, &launches);
+    if (rc) return rc;
     if (fast)
         regen_kernel<true><<<unit_blocks(cfg.keep, 128), 128, 0, st>>>(A, cur, ids, tribes, d_out, d_result);
     else
