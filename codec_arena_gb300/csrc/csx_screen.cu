@@ -238,33 +238,65 @@ void jump_bound(const csx_model &m, JumpBound *jb) {
     }
 }
 
+// The generation's stream split (src/screen.zig:267-297) and the range
+// [t_begin, t_end) of it this call screens (t_end = 0: every stream).
+int split_streams(const csx_cfg &cfg, uint64_t t_begin, uint64_t t_end, StreamGeom &g) {
+    g.seed = cfg.seed;
+    g.T = std::max<uint64_t>(1, std::min<uint64_t>(cfg.threads, cfg.lambda));  // src/screen.zig:267
+    g.per = cfg.lambda / g.T;
+    g.my_last = cfg.lambda - (g.T - 1) * g.per;
+    if (g.T >= 0xFFFFFFFFull) return CSX_ERR_LIMIT;
+    if (t_end == 0) t_end = g.T;  // the whole generation
+    if (t_begin >= t_end || t_end > g.T) return CSX_ERR_BAD_ARGS;
+    g.t0 = t_begin;
+    g.nT = t_end - t_begin;
+    return CSX_OK;
+}
+
+// Mutation form, filter bounds and the CTA list / buffer sizes of a plan.
+void screen_shape(const csx_cfg &cfg, const csx_model &model, bool full, Plan *pl) {
+    pl->fast_delta = std::isfinite(cfg.sigma) && std::fabs(cfg.sigma) <= 1.0e38f &&
+                     (cfg.sigma == 0.0f || std::fabs(cfg.sigma) >= 1.0e-30f);
+    pl->err = filter_bound(model);
+    jump_bound(model, &pl->jb);
+    pl->filter = !full && !(cfg.flags & CSX_FLAG_EXACT_ALL) && pl->err > 0.0f;
+    pl->kpad = std::max<uint32_t>(32, pow2_at_least(cfg.keep));
+    pl->sort_n = pow2_at_least(pl->kpad + 4ull * kThreads);
+    pl->buf_cap = pl->sort_n - pl->kpad;
+}
+
+// Walk segments of about `seg` candidates (g.d_log2 set): L draws rounded to
+// the candidate length when it is constant, the segment counts, and a
+// checkpoint capacity for ck_mult * L / 33 starts.
+void segment_geometry(const csx_cfg &cfg, uint64_t seg, uint64_t ck_mult, StreamGeom &g) {
+    const uint64_t my_max = std::max(g.per, g.my_last);
+    const bool has_last = g.t0 + g.nT == g.T;
+    // candidate length is constant when neither branch probability is mixed
+    const uint32_t it = unit_threshold(cfg.imm_p), jt = unit_threshold(cfg.jump_p);
+    uint64_t gran = 2;
+    if ((it == 0 || it == (1u << 24)) && (jt == 0 || jt == (1u << 24)))
+        gran = (it ? 33 : 62) + (jt ? 2 : 0);
+    uint64_t L = 64 * std::min(seg, my_max);
+    L = ((L + gran - 1) / gran) * gran;
+    g.L = L;
+    g.C = static_cast<uint32_t>(std::max<uint64_t>(1, (64 * g.per + L - 1) / L));
+    g.C_last = static_cast<uint32_t>(std::max<uint64_t>(1, (64 * g.my_last + L - 1) / L));
+    g.n_seg = (g.nT - 1) * g.C + (has_last ? g.C_last : g.C);
+    g.ckcap = static_cast<uint32_t>((ck_mult * L / 33) / (1ull << g.d_log2) + 3);
+}
+
 // grid_override, item_cands, seg_cands: 0 = automatic (the batched screen
 // passes its own grid and the tuner's sizes).
 int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int ne, Plan *pl,
               int grid_override = 0, uint64_t item_cands = 0, uint64_t seg_cands = 0, uint64_t t_begin = 0,
               uint64_t t_end = 0, const csx_model_full *full = nullptr) {
     StreamGeom &g = pl->g;
-    g.seed = cfg.seed;
-    g.T = std::max<uint64_t>(1, std::min<uint64_t>(cfg.threads, cfg.lambda));  // src/screen.zig:267
-    g.per = cfg.lambda / g.T;
-    g.my_last = cfg.lambda - (g.T - 1) * g.per;
+    int src = split_streams(cfg, t_begin, t_end, g);
+    if (src) return src;
     const uint64_t my_max = std::max(g.per, g.my_last);
-    if (g.T >= 0xFFFFFFFFull) return CSX_ERR_LIMIT;
-    if (t_end == 0) t_end = g.T;  // the whole generation
-    if (t_begin >= t_end || t_end > g.T) return CSX_ERR_BAD_ARGS;
-    g.t0 = t_begin;
-    g.nT = t_end - t_begin;
-    const bool has_last = t_end == g.T;
+    const bool has_last = g.t0 + g.nT == g.T;
     const uint64_t lam_range = (g.nT - (has_last ? 1 : 0)) * g.per + (has_last ? g.my_last : 0);
-    pl->fast_delta = std::isfinite(cfg.sigma) && std::fabs(cfg.sigma) <= 1.0e38f &&
-                     (cfg.sigma == 0.0f || std::fabs(cfg.sigma) >= 1.0e-30f);
-    pl->err = filter_bound(model);
-    jump_bound(model, &pl->jb);
-    pl->filter = !full && !(cfg.flags & CSX_FLAG_EXACT_ALL) && pl->err > 0.0f;
-
-    pl->kpad = std::max<uint32_t>(32, pow2_at_least(cfg.keep));
-    pl->sort_n = pow2_at_least(pl->kpad + 4ull * kThreads);
-    pl->buf_cap = pl->sort_n - pl->kpad;
+    screen_shape(cfg, model, full != nullptr, pl);
     const uint32_t tcf = cfg.flags & (CSX_FLAG_TC_BF16 | CSX_FLAG_TC_FP16);
     if (tcf == (CSX_FLAG_TC_BF16 | CSX_FLAG_TC_FP16)) return CSX_ERR_BAD_ARGS;
     if (full && tcf) return CSX_ERR_BAD_ARGS;  // the precision form scores the reference surface
@@ -307,20 +339,7 @@ int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int
     while ((2ull << dl) <= d) ++dl;  // D = 2^dl <= d
     g.d_log2 = dl;
     const uint64_t D = 1ull << dl;
-
-    // candidate length is constant when neither branch probability is mixed
-    const uint32_t it = unit_threshold(cfg.imm_p), jt = unit_threshold(cfg.jump_p);
-    uint64_t gran = 2;
-    if ((it == 0 || it == (1u << 24)) && (jt == 0 || jt == (1u << 24)))
-        gran = (it ? 33 : 62) + (jt ? 2 : 0);
-    const uint64_t seg = seg_cands ? seg_cands : env_u64("CSX_SEG_CANDS", kDefaultSegCands);
-    uint64_t L = 64 * std::min(seg, my_max);
-    L = ((L + gran - 1) / gran) * gran;
-    g.L = L;
-    g.C = static_cast<uint32_t>(std::max<uint64_t>(1, (64 * g.per + L - 1) / L));
-    g.C_last = static_cast<uint32_t>(std::max<uint64_t>(1, (64 * g.my_last + L - 1) / L));
-    g.n_seg = (g.nT - 1) * g.C + (has_last ? g.C_last : g.C);
-    g.ckcap = static_cast<uint32_t>((2 * L / 33) / D + 3);
+    segment_geometry(cfg, seg_cands ? seg_cands : env_u64("CSX_SEG_CANDS", kDefaultSegCands), 2, g);
     pl->short_path = my_max <= D;
     pl->items_cap = pl->short_path ? g.nT : g.n_seg * (static_cast<uint64_t>(g.ckcap) + 1);
     if (pl->items_cap >= 0xFFFFFFFFull) return CSX_ERR_LIMIT;
@@ -791,22 +810,10 @@ int noalloc_setup(int dev, NoAllocDevice **out) {
 // ceil(cnt / D) split points, so items <= 2 * segments + lambda / D.
 int plan_noalloc(const NoAllocDevice &dv, const csx_cfg &cfg, const csx_model &model, int ne, Plan *pl) {
     StreamGeom &g = pl->g;
-    g.seed = cfg.seed;
-    g.T = std::max<uint64_t>(1, std::min<uint64_t>(cfg.threads, cfg.lambda));
-    g.per = cfg.lambda / g.T;
-    g.my_last = cfg.lambda - (g.T - 1) * g.per;
-    g.t0 = 0;
-    g.nT = g.T;
+    int src = split_streams(cfg, 0, 0, g);
+    if (src) return src;
     const uint64_t my_max = std::max(g.per, g.my_last);
-    if (g.T >= 0xFFFFFFFFull) return CSX_ERR_LIMIT;
-    pl->fast_delta = std::isfinite(cfg.sigma) && std::fabs(cfg.sigma) <= 1.0e38f &&
-                     (cfg.sigma == 0.0f || std::fabs(cfg.sigma) >= 1.0e-30f);
-    pl->err = filter_bound(model);
-    jump_bound(model, &pl->jb);
-    pl->filter = !(cfg.flags & CSX_FLAG_EXACT_ALL) && pl->err > 0.0f;
-    pl->kpad = std::max<uint32_t>(32, pow2_at_least(cfg.keep));
-    pl->sort_n = pow2_at_least(pl->kpad + 4ull * kThreads);
-    pl->buf_cap = pl->sort_n - pl->kpad;
+    screen_shape(cfg, model, false, pl);
     pl->smem = screen_smem(pl->sort_n, ne, pl->filter);
     if (pl->smem + 1024 > dv.max_smem) return CSX_ERR_LIMIT;
     int rc = screen_occupancy(screen_fn(pl->fast_delta, pl->filter), dv.num_sms, pl->smem, &pl->grid);
@@ -818,17 +825,7 @@ int plan_noalloc(const NoAllocDevice &dv, const csx_cfg &cfg, const csx_model &m
     while ((2ull << dl) <= d) ++dl;
     g.d_log2 = dl;
     const uint64_t D = 1ull << dl;
-    const uint32_t it = unit_threshold(cfg.imm_p), jt = unit_threshold(cfg.jump_p);
-    uint64_t gran = 2;
-    if ((it == 0 || it == (1u << 24)) && (jt == 0 || jt == (1u << 24)))
-        gran = (it ? 33 : 62) + (jt ? 2 : 0);
-    uint64_t L = 64 * std::min<uint64_t>(kNoAllocSegCands, my_max);
-    L = ((L + gran - 1) / gran) * gran;
-    g.L = L;
-    g.C = static_cast<uint32_t>(std::max<uint64_t>(1, (64 * g.per + L - 1) / L));
-    g.C_last = static_cast<uint32_t>(std::max<uint64_t>(1, (64 * g.my_last + L - 1) / L));
-    g.n_seg = (g.T - 1) * g.C + g.C_last;
-    g.ckcap = static_cast<uint32_t>((L / 33) / D + 3);
+    segment_geometry(cfg, kNoAllocSegCands, 1, g);
     pl->short_path = my_max <= D;
     pl->items_cap = pl->short_path ? g.nT : 2 * g.n_seg + cfg.lambda / D + 1;
     if (pl->items_cap >= 0xFFFFFFFFull) return CSX_ERR_LIMIT;
