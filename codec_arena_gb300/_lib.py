@@ -33,6 +33,8 @@ FLAG_EXACT_ALL = 0x8
 FLAG_STAGE_TIMES = 0x10
 FLAG_TC_BF16 = 0x20
 FLAG_TC_FP16 = 0x40
+FLAG_NO_PRUNE = 0x80
+FLAG_PRUNE_FFMA = 0x100
 
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libcsx_screen.so")
 

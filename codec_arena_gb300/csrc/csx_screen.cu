@@ -51,6 +51,7 @@
 #include "csx_tc.cuh"
 #include "csx_pipeline.cuh"
 #include "csx_screen_kernels.cuh"
+#include "csx_prune.cuh"
 
 namespace csx {
 
@@ -81,7 +82,7 @@ struct Context {
     bool timed = false;
     csx_run_info info{};
     DevBuf genomes, tab, ids, tribes, recs, ck, segout, off, items, lists_a, lists_b, ctrl, surv,
-        result;
+        result, pub;
     // batched islands
     DevBuf batch, b_genomes, b_surv, b_result;
     void *pinned = nullptr;         // host staging of the island descriptors (page-locked)
@@ -139,6 +140,11 @@ struct Plan {
     bool tc = false, fp16 = false;  // precision form (tensor cores + FP64 band)
     float err = 0.0f;
     JumpBound jb{};  // widening of err for a candidate with a jump (filter mode)
+    bool prune = false;     // the pruning screen (csx_prune.cuh)
+    bool prune_tc = false;  // its bound's gradient on the tensor cores
+    int nb = 16;            // crossover genes its bound draws
+    PruneConst pc{};
+    PruneTc ptc{};
 };
 
 int context_init(Context &cx, int dev) {
@@ -260,6 +266,12 @@ void screen_shape(const csx_cfg &cfg, const csx_model &model, bool full, Plan *p
     pl->err = filter_bound(model);
     jump_bound(model, &pl->jb);
     pl->filter = !full && !(cfg.flags & CSX_FLAG_EXACT_ALL) && pl->err > 0.0f;
+    // the pruning screen: the filter form's conditions, the fast delta form
+    // (its mutation is within |sigma| of the parent gene by construction) and
+    // a certifiable bound; the precision form keeps its own kernel
+    pl->prune = pl->filter && pl->fast_delta && !(cfg.flags & CSX_FLAG_NO_PRUNE) &&
+                !(cfg.flags & (CSX_FLAG_TC_BF16 | CSX_FLAG_TC_FP16)) && make_prune(model, cfg.sigma, &pl->pc, &pl->nb);
+    pl->prune_tc = pl->prune && !(cfg.flags & CSX_FLAG_PRUNE_FFMA) && make_prune_tc(model, pl->pc, &pl->ptc);
     pl->kpad = std::max<uint32_t>(32, pow2_at_least(cfg.keep));
     pl->sort_n = pow2_at_least(pl->kpad + 4ull * kThreads);
     pl->buf_cap = pl->sort_n - pl->kpad;
@@ -302,12 +314,28 @@ int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int
     if (full && tcf) return CSX_ERR_BAD_ARGS;  // the precision form scores the reference surface
     pl->tc = tcf != 0;
     pl->fp16 = tcf == CSX_FLAG_TC_FP16;
-    pl->smem = pl->tc ? static_cast<size_t>(pl->sort_n) * sizeof(Entry) +
-                            static_cast<size_t>(ne + 1) * kNtot * sizeof(float) + kTcSmemExtra
-                      : screen_smem(pl->sort_n, ne, pl->filter);
+    if (pl->prune && grid_override == 0) {
+        // the selection scratch holds one key per CTA: at most 8 CTAs of 256 threads per SM
+        pl->smem = prune_smem(pl->sort_n, ne, pl->nb, cx.num_sms, pl->prune_tc);
+        pl->prune = pl->smem + 1024 <= cx.max_smem;
+    } else {
+        pl->prune = false;
+    }
+    if (!pl->prune)
+        pl->smem = pl->tc ? static_cast<size_t>(pl->sort_n) * sizeof(Entry) +
+                                static_cast<size_t>(ne + 1) * kNtot * sizeof(float) + kTcSmemExtra
+                          : screen_smem(pl->sort_n, ne, pl->filter);
     if (pl->smem + 1024 > cx.max_smem) return CSX_ERR_LIMIT;
     if (grid_override > 0) {
         pl->grid = grid_override;
+    } else if (pl->prune) {
+        int rc = screen_occupancy(screen_p_fn(pl->nb, pl->prune_tc), cx.num_sms, pl->smem, &pl->grid);
+        if (rc) return rc;
+        // The occupancy query reports one CTA per SM for the tensor-core form;
+        // its registers (128 at two CTAs), shared memory (~65 KB) and TMEM (32
+        // columns) hold two, which run faster. The screen is persistent with
+        // dynamic work, so any grid is correct.
+        if (pl->prune_tc) pl->grid = std::max(pl->grid, 2 * cx.num_sms);
     } else if (pl->tc) {
         // The occupancy query reports one CTA per SM for this kernel, yet three
         // are resident and run faster (80 registers, ~50 KB of shared memory,
@@ -457,6 +485,7 @@ int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, cons
     const uint32_t nl = static_cast<uint32_t>(pl.grid);
     CSX_CUDA(cx.lists_a.ensure(static_cast<size_t>(nl) * pl.kpad * sizeof(Entry)));
     CSX_CUDA(cx.lists_b.ensure(static_cast<size_t>((nl + 1) / 2) * pl.kpad * sizeof(Entry)));
+    if (pl.prune) CSX_CUDA(cx.pub.ensure(static_cast<size_t>(kPruneMs) * nl * sizeof(uint32_t)));
     if (!pl.short_path) {
         CSX_CUDA(cx.recs.ensure(g.n_seg * sizeof(SegRec)));
         CSX_CUDA(cx.ck.ensure(g.n_seg * g.ckcap * sizeof(uint64_t)));
@@ -475,6 +504,7 @@ int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, cons
     auto mark = [&](int i) -> cudaError_t { return cx.timed ? cudaEventRecord(cx.ev[i], st) : cudaSuccess; };
     CSX_CUDA(mark(0));
     CSX_CUDA(cudaMemsetAsync(ctrl, 0, sizeof(Ctrl), st));
+    if (pl.prune) CSX_CUDA(cudaMemsetAsync(cx.pub.p, 0, static_cast<size_t>(kPruneMs) * nl * sizeof(uint32_t), st));
 
     const SynthConst sc = make_synth(cfg, ne);
 
@@ -509,6 +539,14 @@ int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, cons
         static_cast<ScreenArgs &>(F) = A;
         F.fm = make_full_model(*full);
         screen_full_fn(fast)<<<pl.grid, kThreads, pl.smem, st>>>(F);
+    } else if (pl.prune) {
+        PruneArgs P;
+        static_cast<ScreenArgs &>(P) = A;
+        P.pc = pl.pc;
+        P.tc = pl.ptc;
+        P.pub = static_cast<uint32_t *>(cx.pub.p);
+        P.sel_cap = 8u * static_cast<uint32_t>(cx.num_sms);
+        screen_p_fn(pl.nb, pl.prune_tc)<<<pl.grid, kThreads, pl.smem, st>>>(P);
     } else {
         screen_fn(fast, pl.filter)<<<pl.grid, kThreads, pl.smem, st>>>(A);
     }

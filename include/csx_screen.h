@@ -61,6 +61,13 @@ enum {
                                       survivors ranked by that FP64 score (rounded to f32): the
                                       FP64 top-K, genes bit-exact. csx_screen / csx_screen_device */
 #define CSX_FLAG_TC_FP16 0x40u     /* the same in FP16 with x' = 2g - 1 */
+#define CSX_FLAG_NO_PRUNE 0x80u    /* score every candidate's full synthesis (the filter form)
+                                      instead of skipping, by a certified bound taken after the
+                                      crossover bits, candidates that cannot reach the top-K.
+                                      Results are identical either way; only speed differs */
+#define CSX_FLAG_PRUNE_FFMA 0x100u /* the pruning bound's gradient by FP32 FMA instead of the
+                                      tensor cores (FP16 tcgen05.mma with a certified error
+                                      share). Results are identical either way */
 
 /* Model: the flat weight layout of src/screen.zig:23-27. */
 typedef struct csx_model {
