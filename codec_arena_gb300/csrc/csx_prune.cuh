@@ -49,10 +49,14 @@ struct PruneConst {
 // The bound's gradient on the tensor cores: Qs * 2^-e in FP16 (e chosen so
 // that the largest entry is near 2^15), the canonical no-swizzle K-major tile
 // of csx_tc.cuh; the MMA gives D = Yh Qh with Yh the FP16 parent genes, and
-// grad = wl + 2^e D within PruneTc::err's share (see make_prune_tc).
+// grad = wl + 2^e D within PruneTc::err's share (see make_prune_tc). The
+// bound is centred on yh = fp16(y) itself (|yh - y| <= 2^-12 widens the box),
+// so the thread needs only the packed FP16 genes it hands to the MMA.
 struct PruneTc {
     alignas(16) uint16_t btile[256];
     float dscale;  // 2^e
+    float s;       // half-width around the FP16 centre: PruneConst::s + 2^-12, rounded up
+    float c0;      // PruneConst::c0 at that half-width
     float err;     // replaces PruneConst::err in this form
 };
 
@@ -410,7 +414,7 @@ __device__ __forceinline__ bool tcp_round(TcGroup &g, const uint32_t (&pk)[8], u
 // result, and before TMEM is freed the issuer waits once more (bounded) for
 // the MMA the wait gave up on.
 template <int kNb>
-__global__ void __launch_bounds__(kThreads, 2) screen_pt_kernel(const __grid_constant__ PruneArgs A) {
+__global__ void __launch_bounds__(kThreads, 3) screen_pt_kernel(const __grid_constant__ PruneArgs A) {
     constexpr int kYs = prune_stride<kNb>();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Entry *E = reinterpret_cast<Entry *>(smem_raw);
@@ -568,34 +572,35 @@ __global__ void __launch_bounds__(kThreads, 2) screen_pt_kernel(const __grid_con
 #pragma unroll 1
         for (int r = 0; r < kRounds; ++r) {
             const bool act = valid && !has_def;
-            float y[16];
             uint32_t pk[8];
             float rt = 0.0f;
             PruneHead h{0u, 0u, kNoJump, 0u, false};
             if (act) {
                 const uint64_t s0 = seed_t + (p + 1) * kGolden;
                 h = prune_head(A.sc, s0);
+                float y[16];
                 prune_parents<kNb>(A, yt, s0, h.ea, h.eb, y, rt);
 #pragma unroll
                 for (int j = 0; j < 8; ++j) pk[j] = pack2(y[2 * j], y[2 * j + 1], true);
             } else {
 #pragma unroll
                 for (int j = 0; j < 8; ++j) pk[j] = 0u;
-#pragma unroll
-                for (int i = 0; i < 16; ++i) y[i] = 0.0f;
             }
             float d[16];
             if (!tcp_round(tg, pk, tid & 127u, d, &s_gbad[grp], &s_fail_phase[grp])) tc_ok = false;
             if (act) {
                 float f2 = 0.0f, l1 = 0.0f;
 #pragma unroll
-                for (int k = 0; k < 16; ++k) {
-                    const float gr = __fmaf_rn(d[k], A.tc.dscale, A.m.wlin[k]);
-                    l1 = __fadd_rn(l1, fabsf(gr));
-                    f2 = __fmaf_rn(y[k], __fadd_rn(gr, A.m.wlin[k]), f2);
+                for (int j = 0; j < 8; ++j) {
+                    const float2 yh = __half22float2(*reinterpret_cast<const __half2 *>(&pk[j]));
+                    const float g0 = __fmaf_rn(d[2 * j], A.tc.dscale, A.m.wlin[2 * j]);
+                    const float g1 = __fmaf_rn(d[2 * j + 1], A.tc.dscale, A.m.wlin[2 * j + 1]);
+                    l1 = __fadd_rn(__fadd_rn(l1, fabsf(g0)), fabsf(g1));
+                    f2 = __fmaf_rn(yh.x, __fadd_rn(g0, A.m.wlin[2 * j]), f2);
+                    f2 = __fmaf_rn(yh.y, __fadd_rn(g1, A.m.wlin[2 * j + 1]), f2);
                 }
-                const float b = __fadd_rn(__fmaf_rn(A.pc.s, l1, __fmaf_rn(0.5f, f2, __fadd_rn(A.m.w16, rt))),
-                                          A.pc.c0);
+                const float b = __fadd_rn(__fmaf_rn(A.tc.s, l1, __fmaf_rn(0.5f, f2, __fadd_rn(A.m.w16, rt))),
+                                          A.tc.c0);
                 if (h.imm || !(b < __fsub_rd(tlo, A.jb.c[h.jidx]))) {
                     const unsigned int slot = atomicAdd(&s_pend_n, 1u);
                     if (slot < kPendCap) {
@@ -706,16 +711,17 @@ bool make_prune(const csx_model &m, float sigma, PruneConst *pc, int *nb) {
     return true;
 }
 
-// The tensor-core form's tile and error share for a model whose PruneConst
-// is set. Qs * 2^-e is rounded to FP16 (e: the largest entry lands in
-// (2^14, 2^15]); with yh = fp16(y) (|yh - y| <= 2^-12 for y in [0, 1]), the
-// MMA's exact products and an FP32 accumulation taken as losing at most
-// 2^-18 of its absolute sum,
-//   |2^e D_k - (Qs y)_k| <= eps_k = sum_j (dq_kj + |Qs_kj| 2^-12 + 2^-18 (|Qs_kj| + dq_kj)),
-// dq_kj = |2^e fp16(Qs_kj 2^-e) - Qs_kj| (computed exactly here). The
-// bound uses grad_k = wl_k + 2^e D_k in s sum |grad_k| and in f(y) =
-// 16 w0 + sum_k y_k (grad_k + wl_k) / 2, so it rises by at most
-// (s + 1/2) sum_k eps_k over the exact-gradient bound.
+// The tensor-core form's tile, box and error share for a model whose
+// PruneConst is set. The bound is centred on yh = fp16(y) in [0, 1] (|yh -
+// y| <= 2^-12), so each gene lies within s' = s + 2^-12 of it; c0 takes s'.
+// Qs * 2^-e is rounded to FP16 (e: the largest entry lands in [2^14, 2^15));
+// with the MMA's exact products and an FP32 accumulation taken as losing at
+// most 2^-18 of its absolute sum,
+//   |2^e D_k - (Qs yh)_k| <= eps_k = sum_j (dq_kj + 2^-18 (|Qs_kj| + dq_kj)),
+// dq_kj = |2^e fp16(Qs_kj 2^-e) - Qs_kj| (computed exactly here). The bound
+// uses grad_k = wl_k + 2^e D_k in s' sum |grad_k| and in f(yh) = 16 w0 +
+// sum_k yh_k (grad_k + wl_k) / 2, so it rises by at most (s' + 1/2) sum_k
+// eps_k over the exact-gradient bound at yh.
 bool make_prune_tc(const csx_model &m, const PruneConst &pc, PruneTc *t) {
     double qs[16][16], qmax = 0.0;
     for (int n = 0; n < 16; ++n)
@@ -737,15 +743,25 @@ bool make_prune_tc(const csx_model &m, const PruneConst &pc, PruneTc *t) {
             const double back = std::ldexp(static_cast<double>(__half2float(h)), e);
             if (!std::isfinite(back)) return false;
             const double dq = std::fabs(back - qs[n][k]);
-            eps += dq + std::fabs(qs[n][k]) * std::ldexp(1.0, -12) +
-                   std::ldexp(1.0, -18) * (std::fabs(qs[n][k]) + dq);
+            eps += dq + std::ldexp(1.0, -18) * (std::fabs(qs[n][k]) + dq);
             const int off = (n >> 3) * 256 + (k >> 3) * 128 + (n & 7) * 16 + (k & 7) * 2;
             t->btile[off / 2] = *reinterpret_cast<const uint16_t *>(&h);
         }
-    const double s = static_cast<double>(pc.s);
-    const double err = (static_cast<double>(pc.err) + (s + 0.5) * eps) * (1.0 + std::ldexp(1.0, -20));
-    if (!std::isfinite(err) || err > 1e30) return false;
+    const double up = 1.0 + std::ldexp(1.0, -20);
+    const double s = std::min(static_cast<double>(pc.s) + std::ldexp(1.0, -12), 1.0);
+    double qpos = 0.0, tail = 0.0;
+    for (int i = 0; i < 16; ++i)
+        for (int j = 0; j <= i; ++j) {
+            const double q = static_cast<double>(m.w_quad[i * 16 + j]);
+            qpos += (i == j) ? std::max(q, 0.0) : std::fabs(q);
+        }
+    for (int k = 16; k < kNtot; ++k) tail += std::fabs(static_cast<double>(m.w_lin[k]));
+    const double c0 = (s * tail + s * s * qpos) * up;
+    const double err = (static_cast<double>(pc.err) + (s + 0.5) * eps) * up;
+    if (!std::isfinite(err) || err > 1e30 || !std::isfinite(c0)) return false;
     t->dscale = std::ldexp(1.0f, e);
+    t->s = std::nextafter(static_cast<float>(s), INFINITY);
+    t->c0 = c0 > 0.0 ? std::nextafter(static_cast<float>(c0), INFINITY) : 0.0f;
     t->err = std::nextafter(static_cast<float>(err), INFINITY);
     return true;
 }

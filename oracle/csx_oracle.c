@@ -78,20 +78,25 @@ int orc_model_from_compact(const float *w, int n, orc_model *m) {
 
 /* Model.score with the Zig vector op order: per lane l, acc = w0 + wl*g,
  * sum = sum_i (Wq[i][l] * (g[l]*g[i])) for i = 0..15, then an ordered
- * reduction of acc+sum over the 16 lanes, then + the sequential tail sum. */
+ * reduction of acc+sum over the 16 lanes, then + the sequential tail sum.
+ * The lanes are a 16 x f32 vector as in the reference's @Vector(16, f32)
+ * (GCC vector extension: NEON or SSE/AVX by target, each lane rounding its
+ * own multiply and add; the build forbids contraction). */
+typedef float orc_v16 __attribute__((vector_size(64)));
+
 float orc_score(const orc_model *m, const float *g) {
-    float acc[16], sum[16];
-    for (int l = 0; l < 16; l++) {
-        acc[l] = m->w0 + m->w_lin[l] * g[l];
-        sum[l] = 0.0f;
-    }
+    orc_v16 G, WL, acc, sum = {0};
+    memcpy(&G, g, sizeof(G));
+    memcpy(&WL, m->w_lin, sizeof(WL));
+    acc = m->w0 + WL * G;
     for (int i = 0; i < 16; i++) {
-        const float gi = g[i];
-        const float *wq = &m->w_quad[i * 16];
-        for (int l = 0; l < 16; l++) sum[l] = sum[l] + wq[l] * (g[l] * gi);
+        orc_v16 WQ;
+        memcpy(&WQ, &m->w_quad[i * 16], sizeof(WQ));
+        sum = sum + WQ * (G * g[i]);
     }
+    const orc_v16 t = acc + sum;
     float r = -0.0f;
-    for (int l = 0; l < 16; l++) r = r + (acc[l] + sum[l]);
+    for (int l = 0; l < 16; l++) r = r + t[l];
     float rsum = 0.0f;
     for (int i = 16; i < ORC_NTOT; i++) rsum = rsum + m->w_lin[i] * g[i];
     return r + rsum;
@@ -332,18 +337,27 @@ typedef struct {
     const orc_model_full *mf; /* scores with the full surface when set */
 } orc_ctx;
 
+/* x % d for 32-bit x and 1 <= d < 2^32 without a divide (Lemire, Kaser,
+ * Kurz 2019): m = floor((2^64 - 1) / d) + 1, x % d = hi64((m * x mod 2^64) * d). */
+static inline uint32_t orc_fastmod(uint32_t x, uint64_t m, uint32_t d) {
+    const uint64_t low = m * x;
+    return (uint32_t)(((unsigned __int128)low * d) >> 64);
+}
+
 static float orc_synth(const orc_ctx *c, uint64_t *s, float *g, uint32_t *ea_i, uint32_t *eb_i) {
-    const uint64_t ne = (uint64_t)c->ne;
-    const orc_genome *ea = &c->el[(orc_splitmix_next(s) >> 32) % ne];
-    const orc_genome *eb = &c->el[(orc_splitmix_next(s) >> 32) % ne];
+    const uint32_t ne = (uint32_t)c->ne;
+    const uint64_t mag = ~0ull / ne + 1;
+    const orc_genome *ea = &c->el[orc_fastmod((uint32_t)(orc_splitmix_next(s) >> 32), mag, ne)];
+    const orc_genome *eb = &c->el[orc_fastmod((uint32_t)(orc_splitmix_next(s) >> 32), mag, ne)];
     *ea_i = (uint32_t)(ea - c->el);
     *eb_i = (uint32_t)(eb - c->el);
     if (orc_unit(s) < c->cfg->imm_p) {
         for (int k = 0; k < ORC_NTOT; k++) g[k] = orc_unit(s);
     } else {
         const float sigma = c->cfg->sigma;
+        const float *pa = ea->g, *pb = eb->g;
         for (int k = 0; k < ORC_NTOT; k++) {
-            float v = ((orc_splitmix_next(s) & 1) == 0) ? ea->g[k] : eb->g[k];
+            float v = (orc_splitmix_next(s) & 1) ? pb[k] : pa[k];
             v = v + ((orc_unit(s) - 0.5f) * 2.0f) * sigma;
             g[k] = orc_clamp01(v);
         }
