@@ -236,7 +236,10 @@ __device__ __forceinline__ float next_gene(GeneSource &S, int k) {
 // The filter form leaves the jump out (one compare and select per gene for
 // 2% of candidates): replacing gene j moves the real score by at most
 // JumpBound::c[j], which the caller adds to the bound.
-template <bool kFastDelta, bool kKeepGenes, bool kExact = true, class Model = DevModel>
+// kJump: apply the jump (the exact form and kept genes always do; the filter
+// form leaves it out unless asked, as described above).
+template <bool kFastDelta, bool kKeepGenes, bool kExact = true, class Model = DevModel,
+          bool kJump = kExact || kKeepGenes>
 __device__ __forceinline__ float synth_score(const Model &M, const SynthConst &C,
                                              const float *__restrict__ el, uint64_t seed_t,
                                              uint64_t p, const CandHead &h, float *genes) {
@@ -278,7 +281,7 @@ __device__ __forceinline__ float synth_score(const Model &M, const SynthConst &C
             g = (g != g) ? 1.0f : fmaxf(fminf(g, 1.0f), 0.0f);
         // The filter form scores the genome before the jump; the caller
         // widens its threshold by JumpBound::c[h.jidx] instead.
-        if (kExact || kKeepGenes) g = (static_cast<uint32_t>(k) == h.jidx) ? h.jval : g;
+        if (kJump) g = (static_cast<uint32_t>(k) == h.jidx) ? h.jval : g;
         if (kKeepGenes) genes[k] = g;
         if (!kExact) {
             if (k < 16) {

@@ -132,6 +132,29 @@ __device__ __forceinline__ float prune_bound(const PruneArgs &A, const float *__
     return __fadd_rn(__fmaf_rn(A.pc.s, l1, r), A.pc.c0);
 }
 
+// FP64 score of a queued candidate for the precision form, out of line. Its
+// full synthesis, jump applied, is scored by the FFMA filter first (within
+// ScreenArgs::err of the real score); only a candidate the filter cannot
+// place below tlo = threshold - err is scored in FP64 (rounded to f32, which
+// err covers as well): the FP64 pipe runs at a small fraction of the FP32
+// rate. A filtered-out candidate returns -inf.
+__device__ __noinline__ float prune_rescore64(const ScreenArgs *__restrict__ A, const float *el, uint64_t seed_t,
+                                              uint64_t p, float tlo) {
+    const CandHead h = cand_head(A->sc, seed_t, p);
+    const float sf = synth_score<true, false, false, DevModel, true>(A->m, A->sc, el, seed_t, p, h, nullptr);
+    if (sf < tlo) return -INFINITY;
+    return static_cast<float>(score64_at<true>(&A->m, &A->sc, el, seed_t, p));  // out of line: own registers
+}
+
+// Score of a queued candidate: the reference's f32 order (out of line), or
+// the precision form's FP64 score.
+template <bool kFp64>
+__device__ __forceinline__ float prune_rescore(const ScreenArgs *__restrict__ A, const float *el, uint64_t seed_t,
+                                               uint64_t p, float tlo) {
+    if (!kFp64) return exact_score_at<true>(A, el, seed_t, p);
+    return prune_rescore64(A, el, seed_t, p, tlo);
+}
+
 // The j-th largest (1-based) of v[0..n), by one warp (every lane calls):
 // bisection on the 32-bit key, the largest x with #{v >= x} >= j.
 __device__ __forceinline__ uint32_t warp_kth_largest(const uint32_t *v, uint32_t n, uint32_t j) {
@@ -413,7 +436,11 @@ __device__ __forceinline__ bool tcp_round(TcGroup &g, const uint32_t (&pk)[8], u
 // and the CTA's screening at the next loop head; the error bit voids the
 // result, and before TMEM is freed the issuer waits once more (bounded) for
 // the MMA the wait gave up on.
-template <int kNb>
+// kFp16: the tile format of the bound's MMA (FP16, else BF16). kFp64: the
+// precision form's ranking -- queued candidates are scored in FP64 and rank
+// by that score rounded to f32 (the FP64 top-K; PruneConst::err covers the
+// rounding of those scores too) -- instead of the reference's f32 order.
+template <int kNb, bool kFp16, bool kFp64>
 __global__ void __launch_bounds__(kThreads, 3) screen_pt_kernel(const __grid_constant__ PruneArgs A) {
     constexpr int kYs = prune_stride<kNb>();
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -465,7 +492,7 @@ __global__ void __launch_bounds__(kThreads, 3) screen_pt_kernel(const __grid_con
     tg.tmem_ld = s_tbase + ((32u * (warp & 3u)) << 16) + 16u * grp;
     tg.adesc = tc_sdesc(tg.xs, 128, 256);
     tg.bdesc = tc_sdesc(bts, 128, 256);
-    tg.idesc = tc_idesc(true);
+    tg.idesc = tc_idesc(kFp16);
     tg.bar_id = 1u + grp;
     tg.phase = 0;
     tg.issuer = (tid & 127u) == 0;
@@ -491,7 +518,8 @@ __global__ void __launch_bounds__(kThreads, 3) screen_pt_kernel(const __grid_con
 
     auto rescore = [&](const Pend &q, unsigned long long t1, unsigned long long t2, float ts) {
         const Item it = A.items[q.item];
-        const float s = exact_score_at<true>(&A, el, stream_seed(A.seed, it.stream), it.draw0 + q.ddraw);
+        const float s = prune_rescore<kFp64>(&A, el, stream_seed(A.seed, it.stream), it.draw0 + q.ddraw,
+                                             __fsub_rd(ts, A.err));
         ++exact;
         if (s >= ts) {
             const unsigned long long k1 =
@@ -581,7 +609,7 @@ __global__ void __launch_bounds__(kThreads, 3) screen_pt_kernel(const __grid_con
                 float y[16];
                 prune_parents<kNb>(A, yt, s0, h.ea, h.eb, y, rt);
 #pragma unroll
-                for (int j = 0; j < 8; ++j) pk[j] = pack2(y[2 * j], y[2 * j + 1], true);
+                for (int j = 0; j < 8; ++j) pk[j] = pack2(y[2 * j], y[2 * j + 1], kFp16);
             } else {
 #pragma unroll
                 for (int j = 0; j < 8; ++j) pk[j] = 0u;
@@ -592,7 +620,8 @@ __global__ void __launch_bounds__(kThreads, 3) screen_pt_kernel(const __grid_con
                 float f2 = 0.0f, l1 = 0.0f;
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
-                    const float2 yh = __half22float2(*reinterpret_cast<const __half2 *>(&pk[j]));
+                    const float2 yh = kFp16 ? __half22float2(*reinterpret_cast<const __half2 *>(&pk[j]))
+                                            : __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&pk[j]));
                     const float g0 = __fmaf_rn(d[2 * j], A.tc.dscale, A.m.wlin[2 * j]);
                     const float g1 = __fmaf_rn(d[2 * j + 1], A.tc.dscale, A.m.wlin[2 * j + 1]);
                     l1 = __fadd_rn(__fadd_rn(l1, fabsf(g0)), fabsf(g1));
@@ -651,9 +680,15 @@ __global__ void __launch_bounds__(kThreads, 3) screen_pt_kernel(const __grid_con
 
 using PruneScreenFn = void (*)(PruneArgs);
 
-PruneScreenFn screen_p_fn(int nb, bool tc) {
-    if (tc) return nb > 16 ? screen_pt_kernel<kNtot> : screen_pt_kernel<16>;
-    return nb > 16 ? screen_p_kernel<kNtot> : screen_p_kernel<16>;
+// The pruning kernel of a plan: FFMA or tensor-core bound; for the latter
+// the tile format and the ranking (f32 reference order, or FP64 for the
+// precision form, whose BF16 flag takes BF16 tiles).
+PruneScreenFn screen_p_fn(int nb, bool tc, bool fp16, bool fp64) {
+    const bool t = nb > 16;
+    if (!tc) return t ? screen_p_kernel<kNtot> : screen_p_kernel<16>;
+    if (!fp64) return t ? screen_pt_kernel<kNtot, true, false> : screen_pt_kernel<16, true, false>;
+    if (fp16) return t ? screen_pt_kernel<kNtot, true, true> : screen_pt_kernel<16, true, true>;
+    return t ? screen_pt_kernel<kNtot, false, true> : screen_pt_kernel<16, false, true>;
 }
 
 // Shared memory of the pruning screen: the filter form's, the clamped parent
@@ -712,17 +747,17 @@ bool make_prune(const csx_model &m, float sigma, PruneConst *pc, int *nb) {
 }
 
 // The tensor-core form's tile, box and error share for a model whose
-// PruneConst is set. The bound is centred on yh = fp16(y) in [0, 1] (|yh -
-// y| <= 2^-12), so each gene lies within s' = s + 2^-12 of it; c0 takes s'.
-// Qs * 2^-e is rounded to FP16 (e: the largest entry lands in [2^14, 2^15));
-// with the MMA's exact products and an FP32 accumulation taken as losing at
-// most 2^-18 of its absolute sum,
+// PruneConst is set. The bound is centred on yh = fp16(y) (or bf16(y)) in
+// [0, 1], |yh - y| <= u = 2^-12 (2^-9 for BF16), so each gene lies within
+// s' = s + u of it; c0 takes s'. Qs * 2^-e is rounded to the tile format (e:
+// the largest entry lands in [2^14, 2^15)); with the MMA's exact products
+// and an FP32 accumulation taken as losing at most 2^-18 of its absolute sum,
 //   |2^e D_k - (Qs yh)_k| <= eps_k = sum_j (dq_kj + 2^-18 (|Qs_kj| + dq_kj)),
-// dq_kj = |2^e fp16(Qs_kj 2^-e) - Qs_kj| (computed exactly here). The bound
+// dq_kj = |2^e round(Qs_kj 2^-e) - Qs_kj| (computed exactly here). The bound
 // uses grad_k = wl_k + 2^e D_k in s' sum |grad_k| and in f(yh) = 16 w0 +
 // sum_k yh_k (grad_k + wl_k) / 2, so it rises by at most (s' + 1/2) sum_k
 // eps_k over the exact-gradient bound at yh.
-bool make_prune_tc(const csx_model &m, const PruneConst &pc, PruneTc *t) {
+bool make_prune_tc(const csx_model &m, const PruneConst &pc, bool fp16, PruneTc *t) {
     double qs[16][16], qmax = 0.0;
     for (int n = 0; n < 16; ++n)
         for (int k = 0; k < 16; ++k) {
@@ -739,16 +774,25 @@ bool make_prune_tc(const csx_model &m, const PruneConst &pc, PruneTc *t) {
     for (int n = 0; n < 16; ++n)
         for (int k = 0; k < 16; ++k) {
             const float x = static_cast<float>(std::ldexp(qs[n][k], -e));  // exact: a power-of-two scaling
-            const __half h = __float2half_rn(x);
-            const double back = std::ldexp(static_cast<double>(__half2float(h)), e);
+            uint16_t bits;
+            double back;
+            if (fp16) {
+                const __half h = __float2half_rn(x);
+                bits = *reinterpret_cast<const uint16_t *>(&h);
+                back = std::ldexp(static_cast<double>(__half2float(h)), e);
+            } else {
+                const __nv_bfloat16 h = __float2bfloat16_rn(x);
+                bits = *reinterpret_cast<const uint16_t *>(&h);
+                back = std::ldexp(static_cast<double>(__bfloat162float(h)), e);
+            }
             if (!std::isfinite(back)) return false;
             const double dq = std::fabs(back - qs[n][k]);
             eps += dq + std::ldexp(1.0, -18) * (std::fabs(qs[n][k]) + dq);
             const int off = (n >> 3) * 256 + (k >> 3) * 128 + (n & 7) * 16 + (k & 7) * 2;
-            t->btile[off / 2] = *reinterpret_cast<const uint16_t *>(&h);
+            t->btile[off / 2] = bits;
         }
     const double up = 1.0 + std::ldexp(1.0, -20);
-    const double s = std::min(static_cast<double>(pc.s) + std::ldexp(1.0, -12), 1.0);
+    const double s = std::min(static_cast<double>(pc.s) + std::ldexp(1.0, fp16 ? -12 : -9), 1.0);
     double qpos = 0.0, tail = 0.0;
     for (int i = 0; i < 16; ++i)
         for (int j = 0; j <= i; ++j) {

@@ -269,9 +269,15 @@ void screen_shape(const csx_cfg &cfg, const csx_model &model, bool full, Plan *p
     // the pruning screen: the filter form's conditions, the fast delta form
     // (its mutation is within |sigma| of the parent gene by construction) and
     // a certifiable bound; the precision form keeps its own kernel
+    // a certifiable bound. The precision form (TC flags) prunes with its tile
+    // format's bound and ranks in FP64; without a tensor-core bound it keeps
+    // its own unpruned kernel.
+    const uint32_t tcf = cfg.flags & (CSX_FLAG_TC_BF16 | CSX_FLAG_TC_FP16);
     pl->prune = pl->filter && pl->fast_delta && !(cfg.flags & CSX_FLAG_NO_PRUNE) &&
-                !(cfg.flags & (CSX_FLAG_TC_BF16 | CSX_FLAG_TC_FP16)) && make_prune(model, cfg.sigma, &pl->pc, &pl->nb);
-    pl->prune_tc = pl->prune && !(cfg.flags & CSX_FLAG_PRUNE_FFMA) && make_prune_tc(model, pl->pc, &pl->ptc);
+                make_prune(model, cfg.sigma, &pl->pc, &pl->nb);
+    pl->prune_tc = pl->prune && (tcf != 0 || !(cfg.flags & CSX_FLAG_PRUNE_FFMA)) &&
+                   make_prune_tc(model, pl->pc, tcf != CSX_FLAG_TC_BF16, &pl->ptc);
+    if (tcf && !pl->prune_tc) pl->prune = false;
     pl->kpad = std::max<uint32_t>(32, pow2_at_least(cfg.keep));
     pl->sort_n = pow2_at_least(pl->kpad + 4ull * kThreads);
     pl->buf_cap = pl->sort_n - pl->kpad;
@@ -312,7 +318,7 @@ int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int
     const uint32_t tcf = cfg.flags & (CSX_FLAG_TC_BF16 | CSX_FLAG_TC_FP16);
     if (tcf == (CSX_FLAG_TC_BF16 | CSX_FLAG_TC_FP16)) return CSX_ERR_BAD_ARGS;
     if (full && tcf) return CSX_ERR_BAD_ARGS;  // the precision form scores the reference surface
-    pl->tc = tcf != 0;
+    pl->tc = tcf != 0;  // FP64 ranking (pruned, or the unpruned precision kernel)
     pl->fp16 = tcf == CSX_FLAG_TC_FP16;
     if (pl->prune && grid_override == 0) {
         // the selection scratch holds one key per CTA: at most 8 CTAs of 256 threads per SM
@@ -329,7 +335,8 @@ int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int
     if (grid_override > 0) {
         pl->grid = grid_override;
     } else if (pl->prune) {
-        int rc = screen_occupancy(screen_p_fn(pl->nb, pl->prune_tc), cx.num_sms, pl->smem, &pl->grid);
+        int rc = screen_occupancy(screen_p_fn(pl->nb, pl->prune_tc, pl->fp16 || !pl->tc, pl->tc), cx.num_sms,
+                                  pl->smem, &pl->grid);
         if (rc) return rc;
         // The occupancy query reports one CTA per SM for the tensor-core form;
         // its registers (80 at three CTAs), shared memory (~65 KB each) and
@@ -526,7 +533,15 @@ int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, cons
     CSX_CUDA(mark(2));
 
     const ScreenArgs A = screen_args(cfg, model, sc, pl, tab, items, ctrl, static_cast<Entry *>(cx.lists_a.p));
-    if (pl.tc) {
+    if (pl.prune) {
+        PruneArgs P;
+        static_cast<ScreenArgs &>(P) = A;
+        P.pc = pl.pc;
+        P.tc = pl.ptc;
+        P.pub = static_cast<uint32_t *>(cx.pub.p);
+        P.sel_cap = 8u * static_cast<uint32_t>(cx.num_sms);
+        screen_p_fn(pl.nb, pl.prune_tc, pl.fp16 || !pl.tc, pl.tc)<<<pl.grid, kThreads, pl.smem, st>>>(P);
+    } else if (pl.tc) {
         TcScreenArgs P;
         P.A = A;
         P.band = kTcBand;
@@ -540,14 +555,6 @@ int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, cons
         static_cast<ScreenArgs &>(F) = A;
         F.fm = make_full_model(*full);
         screen_full_fn(fast)<<<pl.grid, kThreads, pl.smem, st>>>(F);
-    } else if (pl.prune) {
-        PruneArgs P;
-        static_cast<ScreenArgs &>(P) = A;
-        P.pc = pl.pc;
-        P.tc = pl.ptc;
-        P.pub = static_cast<uint32_t *>(cx.pub.p);
-        P.sel_cap = 8u * static_cast<uint32_t>(cx.num_sms);
-        screen_p_fn(pl.nb, pl.prune_tc)<<<pl.grid, kThreads, pl.smem, st>>>(P);
     } else {
         screen_fn(fast, pl.filter)<<<pl.grid, kThreads, pl.smem, st>>>(A);
     }

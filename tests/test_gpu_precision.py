@@ -138,3 +138,30 @@ def test_tc_screen_deterministic_and_counts():
     b, nb = screen.screen(cfg, screen.Model.from_compact(w), el)
     assert na == nb == 3_000_000
     assert a.tobytes() == b.tobytes()
+
+
+@pytest.mark.parametrize("form", ["bf16", "fp16"])
+def test_pruned_precision_form_equals_unpruned(form):
+    """The precision form prunes with its tile format's bound and ranks queued
+    candidates by their FP64 score; the unpruned precision kernel
+    (CSX_FLAG_NO_PRUNE) scores every candidate on the tensor cores with an FP64
+    band. Both certify the FP64 top-K, so their survivors are the same bytes,
+    on the committed surface, a surface with linear weights past gene 15 and
+    elites with genes outside [0, 1]."""
+    from codec_arena_gb300 import _lib, screen, workloads as wl
+
+    flag = _lib.FLAG_TC_BF16 if form == "bf16" else _lib.FLAG_TC_FP16
+    rng = np.random.default_rng(12)
+    tail = rng.normal(0, 1, 166).astype(np.float32)
+    tail[17:30] = rng.normal(0, 20, 13).astype(np.float32)
+    odd = wl.seeded_elites(12)
+    odd["g"][0, :5] = [-0.0, -3.0, 7.5, np.inf, -np.inf]
+    odd["g"][1, :3] = [np.nan, 1.0, 0.0]
+    for w, el, lam, K, T in ((wl.surrogate_161(), wl.seeded_elites(64), 3_000_000, 256, 4),
+                             (tail, wl.seeded_elites(64), 1_000_000, 64, 7),
+                             (wl.surrogate_161(), odd, 1_000_000, 100, 3)):
+        m = screen.Model.from_compact(w)
+        a, na = screen.screen(screen.Cfg(lam, K, 5, threads=T, flags=flag), m, el)
+        b, nb = screen.screen(screen.Cfg(lam, K, 5, threads=T, flags=flag | _lib.FLAG_NO_PRUNE), m, el)
+        assert na == nb == lam and len(a) == K
+        assert a.tobytes() == b.tobytes()
