@@ -52,10 +52,23 @@ KEEP = 256
 THREADS = 4
 SEED = 7
 N_ELITES = 64
-# Algorithmic 32-bit lane-ops per candidate: 61.75 splitmix64 draws x 20 +
-# 29 genes x 5 + 181 FMA x 2: the candidate's RNG, gene arithmetic and scoring.
+# Algorithmic 32-bit lane-ops per candidate of the full synthesis: 61.75
+# splitmix64 draws x 20 + 29 genes x 5 + 181 FMA x 2: the candidate's RNG, gene
+# arithmetic and scoring (the unpruned form).
 LANE_OPS_PER_CAND = 1760.0
 DRAWS_PER_CAND = 61.75
+# The pruning form per candidate: the header's 4 draws (parents, immigrant
+# test, jump test) + 0.02 jump index draws, the 16 crossover-bit draws of the
+# 0.99 crossover candidates (x 20 lane-ops each), the bound's FP32 work on them
+# (4 x 16 lane-ops beside the tensor core's 16 x 16 MACs, 8 packs), and the
+# full 1760 for the fraction q queued for the reference-order score.
+PRUNE_DRAWS = 4.02 + 0.99 * 16
+PRUNE_FIXED_OPS = PRUNE_DRAWS * 20 + 0.99 * (4 * 16 + 8)
+PRUNE_TC_FLOP = 0.99 * 2 * 16 * 16  # tensor-core flops per candidate (the bound's gradient)
+
+
+def prune_ops(q):
+    return PRUNE_FIXED_OPS + q * LANE_OPS_PER_CAND
 
 
 def parse(argv=None):
@@ -71,8 +84,10 @@ def parse(argv=None):
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-precision", action="store_true", help="skip the tensor-core precision forms")
     ap.add_argument("--workload", default="generation",
-                    choices=["generation", "islands", "precision", "refit", "full"],
-                    help="islands: 20 islands batched in one graph launch (not the headline line)")
+                    choices=["generation", "islands", "precision", "refit", "full", "config1"],
+                    help="islands: 20 islands batched in one graph launch (not the headline line); "
+                         "config1: the reference workload's first configuration (lambda 1e6, top 32, "
+                         "seeded 153-term surface)")
     ap.add_argument("--islands", type=int, default=20)
     ap.add_argument("--islands-scale", type=float, default=1.0,
                     help="scale every island budget (small cases for profiling)")
@@ -84,7 +99,20 @@ def dist_env():
         int(os.environ.get("LOCAL_RANK", 0))
 
 
+def _config1_args(args):
+    """The reference workload's first configuration: lambda 1e6, top 32."""
+    args.lam, args.keep = 1_000_000, 32
+
+
 def workload_config(args, n):
+    if args.workload == "config1":
+        return {"workload": f"the reference workload's first configuration: lambda={args.lam} candidates, "
+                            f"{N_ELITES} elites drawn from seed 1, 153-coefficient surface drawn N(0,1) x 0.1 "
+                            f"from seed 2, top-{args.keep}, T={args.threads} RNG streams",
+                "lambda": args.lam, "keep": args.keep, "threads": args.threads, "elites": N_ELITES,
+                "surrogate": "seeded N(0,1) x 0.1, 153 coefficients (v1 layout), seed 2", "sigma": 0.12,
+                "jump_p": 0.02, "imm_p": 0.01, "seed": SEED,
+                "l2": "flushed between steps (256 MiB write)", "parallelism": "single"}
     return {"workload": f"screen generation: lambda={args.lam} candidates, {N_ELITES} seeded elites, "
                         f"committed v3 surrogate (161 coefficients), top-{args.keep}, "
                         f"T={args.threads} RNG streams" + (f", {n} islands" if n > 1 else ""),
@@ -190,8 +218,11 @@ def run_reference(args):
 
     from codec_arena_gb300 import workloads as wl
 
+    if args.workload == "config1":
+        _config1_args(args)
     el = wl.seeded_elites(N_ELITES)
-    m = oracle.model_from_compact(wl.surrogate_161())
+    w = wl.seeded_normal_model(seed=2) if args.workload == "config1" else wl.surrogate_161()
+    m = oracle.model_from_compact(w)
     T = args.threads
     # bounded sample per step: the T-stream prefix that takes ~2 s on T threads
     lam = 400_000
@@ -214,7 +245,11 @@ def run_reference(args):
             "ms_per_step": 1000 * tot / steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": v / PUBLISHED_CAND_S, "vs_baseline_source": PUBLISHED_SOURCE,
             "dtype": "u64/f32", "data": "synthetic (seeded)",
-            "config": workload_config(args, 1),
+            "config": dict(workload_config(args, 1),
+                           sample=f"each timed step screens the first {lam // T} candidates of each of the "
+                                  f"T={T} streams ({lam} of the {args.lam} candidates; a stream's content does "
+                                  "not depend on lambda, so the rate is the generation's); ms_per_step is that "
+                                  "sample's time"),
             "cpu_baseline": {"value": v, "unit": "candidates/s", "cores": T, "kind": "port",
                              "sample": f"each step: first {lam // T} candidates of each of T={T} "
                                        f"streams ({lam} candidates) on {T} threads; Zig is not "
@@ -311,6 +346,16 @@ PUBLISHED_CAND_S = 17.2e6
 PUBLISHED_SOURCE = "17.2 M candidates/s, Zig SIMD screen, 4 threads (docs/SCALE.md:26)"
 
 
+def _profile_summary() -> dict:
+    """ncu figures of the default screen kernel kept under profiles/ (DRAM
+    traffic per launch scaled to the full workload, pipe utilisation)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "screen_pt_kernel_ncu.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
 def _measured_peaks() -> dict:
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -346,10 +391,24 @@ def issue_slots(achieved_tops, clocks):
             "peak_source": f"issue limit: 4 schedulers x 32 lanes x {sms} SMs x {mhz:.0f} MHz"}
 
 
-def precision_forms(args, fp32_surv=None):
-    """BF16 and FP16 tensor-core screens of the generation workload beside the
-    plain FP32 screen: throughput (CUDA events, L2 flushed), top-K recall
-    against the FP64 top-K, and score errors against FP64."""
+FORMS = (
+    ("fp32_unpruned", "FLAG_NO_PRUNE", "every candidate synthesised and scored (FFMA filter, reference f32 "
+                                       "order near the threshold): the plain FP32 form"),
+    ("fp32_prune_ffma", "FLAG_PRUNE_FFMA", "pruning, the bound's gradient by FP32 FMA; reference f32 order"),
+    ("bf16_tc", "FLAG_TC_BF16", "precision form: pruning bound on BF16 tensor cores, queued candidates "
+                                "filtered by FFMA and scored in FP64, survivors the FP64 top-K"),
+    ("fp16_tc", "FLAG_TC_FP16", "precision form as bf16_tc with FP16 tiles"),
+    ("bf16_tc_unpruned", "FLAG_TC_BF16|FLAG_NO_PRUNE", "precision form without pruning: the quadratic "
+                                                        "block of every candidate on BF16 tensor cores, an "
+                                                        "FP64 band"),
+)
+
+
+def precision_forms(args, default=None):
+    """The generation in each form beside the default (pruned, FP16 tensor-core
+    bound, reference f32 order): throughput (CUDA events, L2 flushed), screen
+    kernel time, candidates rescored, top-K recall against the FP64 top-K,
+    and the tensor-core scores' errors against FP64."""
     import numpy as np
     import torch
 
@@ -360,10 +419,13 @@ def precision_forms(args, fp32_surv=None):
     d_el = torch.from_numpy(el.view(np.uint8).copy()).cuda()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     out = {}
-    forms = (("bf16_tc", _lib.FLAG_TC_BF16), ("fp16_tc", _lib.FLAG_TC_FP16))
-    if fp32_surv is None:
-        forms = (("fp32_plain", 0),) + forms
-    for name, flag in forms:
+    forms = list(FORMS)
+    if default is None:
+        forms.insert(0, ("fp32_prune_tc", "", "default: pruning, the bound's gradient on FP16 tensor cores"))
+    for name, flagnames, what in forms:
+        flag = 0
+        for fn in filter(None, flagnames.split("|")):
+            flag |= getattr(_lib, fn)
         cfg = screen.Cfg(args.lam, args.keep, SEED, threads=args.threads, flags=flag | _lib.FLAG_STAGE_TIMES)
         d_out = torch.zeros(args.keep * 168, dtype=torch.uint8, device="cuda")
         d_res = torch.zeros(4, dtype=torch.int64, device="cuda")
@@ -382,17 +444,24 @@ def precision_forms(args, fp32_surv=None):
         res = d_res.cpu().numpy()
         assert res[2] == 0 and res[1] == args.lam
         info = screen.last_run_info()
-        out[name] = {"value": args.lam / (statistics.mean(ms) / 1000), "ms_per_step": statistics.mean(ms),
-                     "screen_kernel_ms": statistics.mean(kms), "rescored": info["exact_evals"],
-                     "screen_ctas": info["screen_ctas"],
+        out[name] = {"form": what, "flags": flagnames or "0", "value": args.lam / (statistics.mean(ms) / 1000),
+                     "ms_per_step": statistics.mean(ms), "screen_kernel_ms": statistics.mean(kms),
+                     "rescored": info["exact_evals"], "screen_ctas": info["screen_ctas"],
                      "_surv": screen.survivors_from_bytes(d_out.cpu().numpy(), int(res[0]))}
-        if flag:  # tensor work of the form: one 128x16x16 MMA per 128 candidates = 512 flop per candidate
-            tf = 512.0 * args.lam / (statistics.mean(kms) * 1e-3) / 1e12
+        if "TC" in flagnames:
+            # tensor work: pruned forms 2 x 16 x 16 flop per crossover candidate (the bound's
+            # gradient), the unpruned form one 128x16x16 MMA per 128 candidates (512 flop)
+            flop = 512.0 if "NO_PRUNE" in flagnames else PRUNE_TC_FLOP
+            tf = flop * args.lam / (statistics.mean(kms) * 1e-3) / 1e12
             pk = _measured_peaks().get("bf16_tflops") or 1900.0
             out[name]["tensor_roofline"] = {"achieved": tf, "peak": pk, "unit": "TFLOP/s", "frac": tf / pk,
-                                            "note": "the form stays bound by the integer synthesis"}
-    if fp32_surv is not None:
-        out["fp32_plain"] = {"_surv": fp32_surv}
+                                            "note": "the tensor cores carry a 16x16 product per candidate; "
+                                                    "the form stays bound by the integer synthesis"}
+    if default is not None:
+        v, ms_step, kms_, rescored, surv = default
+        out["fp32_prune_tc"] = {"form": "default: pruning, the bound's gradient on FP16 tensor cores (the line's "
+                                        "value)", "flags": "0", "value": v, "ms_per_step": ms_step,
+                                "screen_kernel_ms": kms_, "rescored": rescored, "_surv": surv}
     # FP64 ground truth: the exact screen's top 4096 rescored in FP64, certified complete below
     big, _ = screen.screen(screen.Cfg(args.lam, 4096, SEED, threads=args.threads), model, el)
     s64 = _fp64_scores(model, big["g"])
@@ -403,18 +472,23 @@ def precision_forms(args, fp32_surv=None):
     A = 16 * abs(float(model.w0)) + np.abs(model.w_lin).sum() + np.abs(L).sum()
     e32 = 36 * 2.0 ** -24 * A  # the exact order's FP32 error bound (gamma_35 of the absolute terms)
     certified = bool(float(big["score"][-1]) + e32 < s64[order[K - 1]])
+    ref = out["fp32_prune_tc"]["_surv"].tobytes()
     for name in out:
-        have = {(int(r["stream"]), int(r["index"])) for r in out[name].pop("_surv")}
+        sv = out[name].pop("_surv")
+        have = {(int(r["stream"]), int(r["index"])) for r in sv}
         out[name]["recall_vs_fp64"] = len(have & truth) / K
+        if name.startswith("fp32"):
+            out[name]["identical_to_default"] = sv.tobytes() == ref
     g_top = torch.from_numpy(np.ascontiguousarray(big["g"])).cuda()
     rng = np.random.default_rng(5)
     g_rand = rng.random((1_000_000, 29), dtype=np.float32)
     s64_rand = _fp64_scores(model, g_rand)
     g_rand = torch.from_numpy(g_rand).cuda()
     for form in ("bf16", "fp16"):
+        # the tensor-core score (csx_tc_score, the unpruned precision form's) against FP64
         e_top = np.abs(precision.tc_score(model, g_top, form).cpu().numpy() - s64)
         e_rand = np.abs(precision.tc_score(model, g_rand, form).cpu().numpy() - s64_rand)
-        out[form + "_tc"]["score_error_vs_fp64"] = {
+        out[form + "_tc"]["tc_score_error_vs_fp64"] = {
             "max_abs_top4096": float(e_top.max()), "mean_abs_top4096": float(e_top.mean()),
             "max_rel_top4096": float((e_top / np.abs(s64)).max()),
             "max_abs_uniform1e6": float(e_rand.max()), "mean_abs_uniform1e6": float(e_rand.mean())}
@@ -436,8 +510,10 @@ def run_precision(args):
             "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": f["bf16_tc"]["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": f["bf16_tc"]["value"] / PUBLISHED_CAND_S,
             "vs_baseline_source": PUBLISHED_SOURCE,
-            "dtype": "bf16 tensor cores + f64 band; genes u64/f32", "data": "synthetic (seeded)",
-            "config": workload_config(args, 1), "bf16_over_fp32": f["bf16_tc"]["value"] / f["fp32_plain"]["value"],
+            "dtype": "bf16 tensor cores (pruning bound) + f64 ranking; genes u64/f32", "data": "synthetic (seeded)",
+            "config": workload_config(args, 1),
+            "bf16_over_fp32": f["bf16_tc"]["value"] / f["fp32_unpruned"]["value"],
+            "bf16_over_fp32_pruned": f["bf16_tc"]["value"] / f["fp32_prune_tc"]["value"],
             "clocks": clocks}
     line.update(p)
     print(json.dumps(line), flush=True)
@@ -606,8 +682,77 @@ def run_full(args):
     print(json.dumps(line), flush=True)
 
 
+def run_config1(args):
+    """`--workload config1`: the reference workload's first configuration
+    (lambda 1e6, top 32, 64 elites from seed 1, the seeded 153-term surface)
+    through the same pipeline, the device-resident value and the host-buffer
+    e2e, beside the oracle on the host cores."""
+    import numpy as np
+    import torch
+
+    from codec_arena_gb300 import _lib, screen, workloads as wl
+
+    _config1_args(args)
+    torch.cuda.set_device(0)
+    el = wl.seeded_elites(N_ELITES, seed=1)
+    w = wl.seeded_normal_model(seed=2)
+    model = screen.Model.from_compact(w)
+    cfg = screen.Cfg(args.lam, args.keep, SEED, threads=args.threads, flags=_lib.FLAG_STAGE_TIMES)
+    d_el = torch.from_numpy(el.view(np.uint8).copy()).cuda()
+    d_out = torch.zeros(args.keep * _lib.SURVIVOR_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    d_res = torch.zeros(4, dtype=torch.int64, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(max(3, args.warmup)):
+        screen.screen_device(cfg, model, d_el, d_out, d_res)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(0)
+    sampler.start()
+    ms = []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        screen.screen_device(cfg, model, d_el, d_out, d_res)
+        b.record()
+        b.synchronize()
+        ms.append(a.elapsed_time(b))
+    clocks = sampler.stop()
+    res = d_res.cpu().numpy()
+    assert res[2] == 0 and res[1] == args.lam, f"device result {res}"
+    info = screen.last_run_info()
+    hcfg = screen.Cfg(args.lam, args.keep, SEED, threads=args.threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        surv, _ = screen.screen(hcfg, model, el)
+    e2e_t = (time.perf_counter() - t0) / args.steps
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    t0 = time.perf_counter()
+    want, _ = oracle.screen(oracle.cfg(args.lam, args.keep, SEED, threads=args.threads),
+                            oracle.model_from_compact(w), el, cpu_threads=args.threads)
+    cpu_s = time.perf_counter() - t0
+    value = args.lam / (statistics.mean(ms) / 1000.0)
+    line = {"metric": METRIC, "value": value, "unit": "candidates/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": statistics.mean(ms), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": value / PUBLISHED_CAND_S, "vs_baseline_source": PUBLISHED_SOURCE,
+            "dtype": "u64/f32", "data": "synthetic (seeded)", "config": workload_config(args, 1),
+            "e2e": {"value": args.lam / e2e_t, "unit": "candidates/s", "h2d_bytes_per_step": int(el.nbytes),
+                    "d2h_bytes_per_step": int(len(surv) * _lib.SURVIVOR_DTYPE.itemsize + 32),
+                    "api": "csx_screen (host buffers, synchronous)"},
+            "identical_to_oracle": surv.tobytes() == want.tobytes(),
+            "stages_ms_last_step": {k: round(v, 4) for k, v in info.items() if k.startswith("ms_")},
+            "cpu_baseline": {"value": args.lam / cpu_s, "unit": "candidates/s", "cores": args.threads,
+                             "kind": "port", "sample": f"the whole configuration ({args.lam} candidates, "
+                                                       f"{cpu_s:.2f} s) on {args.threads} threads"},
+            "clocks": clocks, "gpu_launches": int(info["launches"]) * args.steps}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "config1" and args.impl != "reference":
+        return run_config1(args)
     if args.workload == "refit" and args.impl != "reference":
         return run_refit(args)
     if args.workload == "full" and args.impl != "reference":
@@ -707,34 +852,37 @@ def main():
             rates[name] = r.value
     ms_screen = statistics.mean(screen_ms)
     cand_s_kernel = args.lam / (ms_screen / 1000.0)
-    achieved = cand_s_kernel * LANE_OPS_PER_CAND / 1e12
-    peak = rates.get("int_alu", 0.0) / 1e12
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "screen_kernel_traffic.json")
-    if os.path.exists(tpath):
-        try:
-            traffic = json.load(open(tpath)).get("bytes_per_launch_full_workload")
-        except Exception:
-            traffic = None
+    q = statistics.mean(st["exact_evals"] for st in stage) / args.lam  # queued for the reference order
+    ops = prune_ops(q)
+    achieved = cand_s_kernel * ops / 1e12
+    slots = issue_slots(achieved, clocks)
+    prof = _profile_summary()
+    traffic = prof.get("bytes_per_launch_full_workload") if args.lam == LAMBDA else None
+    tc_tf = cand_s_kernel * PRUNE_TC_FLOP / 1e12
+    bf16_peak = _measured_peaks().get("bf16_tflops")
     roofline = {
-        "bound": "int-issue", "kernel": "csx::screen_q_kernel<true>",
-        "achieved": achieved, "peak": peak, "unit": "Tlane-op/s",
-        "frac": achieved / peak if peak else None, "traffic": traffic,
-        "algorithmic_ops_per_candidate": LANE_OPS_PER_CAND,
-        "peak_source": "measured: integer ALU issue rate of this GPU (csx_bench_issue_rate kind 0)",
-        "splitmix64_bound": {"hashes_per_s": rates.get("splitmix64"),
-                             "achieved_hashes_per_s": cand_s_kernel * DRAWS_PER_CAND,
-                             "frac": (cand_s_kernel * DRAWS_PER_CAND / rates["splitmix64"])
-                             if rates.get("splitmix64") else None},
-        "issue_rates_measured": rates,
-        "issue_slots": issue_slots(achieved, clocks),
+        "bound": "int-issue", "kernel": prof.get("kernel", "csx::screen_pt_kernel<16, true, false>"),
+        "achieved": achieved, "peak": slots["peak"], "unit": "Tlane-op/s", "frac": slots["frac"],
+        "peak_source": slots.get("peak_source"),
+        "algorithmic_ops_per_candidate": ops,
+        "ops_model": ("pruning form: %.2f draws x 20 lane-ops (4 header draws, 0.02 jump index, 16 crossover "
+                      "bits for the 0.99 crossover candidates) + 0.99 x 72 bound lane-ops + q x 1760 for the "
+                      "fraction q queued for the full synthesis and reference-order score (measured q)"
+                      % PRUNE_DRAWS),
+        "queued_fraction": q,
+        "traffic": traffic,
+        "traffic_source": prof.get("traffic_note"),
         "kernel_ms_per_launch": ms_screen,
-        # the other two ceilings, for completeness: HBM (the launch's DRAM
-        # traffic against the measured copy bandwidth) -- the kernel is far
-        # from it -- and the tensor cores, which the plain form does not use
+        "ncu": prof.get("ncu"),
+        "issue_rates_measured": rates,
+        "alu_probe_frac": (achieved / (rates["int_alu"] / 1e12)) if rates.get("int_alu") else None,
+        # the other two ceilings: HBM (the launch's DRAM traffic against the
+        # measured copy bandwidth) and the tensor pipe (the bound's gradient:
+        # 2 x 16 x 16 flop per crossover candidate)
         "hbm": hbm_ceiling(traffic, ms_screen),
-        "tensor": {"achieved": 0.0, "unit": "TFLOP/s", "peak": _measured_peaks().get("bf16_tflops"),
-                   "frac": 0.0, "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)"},
+        "tensor": {"achieved": tc_tf, "unit": "TFLOP/s", "peak": bf16_peak,
+                   "frac": tc_tf / bf16_peak if bf16_peak else None,
+                   "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)"},
     }
     line = {"metric": METRIC, "value": value, "unit": "candidates/s",
             "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
@@ -747,14 +895,26 @@ def main():
             "shape": dict({k: stage[-1][k] for k in ("screen_ctas", "segments", "seg_draws", "item_cands")},
                           items=int(res[3])),
             "exact_evals_last_step": stage[-1]["exact_evals"],
+            "form": "pruning screen: bound's gradient on the FP16 tensor cores, survivors in the reference's "
+                    "f32 order (byte-identical to the unpruned screen)",
             "wall_s": wall}
     if world == 1 and not args.no_precision:
-        # the BF16 / FP16 tensor-core forms of the same generation, beside this plain FP32 value
+        # the other forms of the same generation beside this value: unpruned
+        # FP32, the FFMA bound, and the BF16 / FP16 precision forms
         line["precision_forms"] = precision_forms(
-            args, fp32_surv=screen.survivors_from_bytes(d_out.cpu().numpy(), int(d_res[0].item())))
+            args, default=(value, line["ms_per_step"], ms_screen, stage[-1]["exact_evals"],
+                           screen.survivors_from_bytes(d_out.cpu().numpy(), int(d_res[0].item()))))
         f = line["precision_forms"]["forms"]
-        f["fp32_plain"].update({"value": value, "ms_per_step": line["ms_per_step"]})
-        line["bf16_over_fp32"] = f["bf16_tc"]["value"] / value
+        line["bf16_over_fp32"] = f["bf16_tc"]["value"] / f["fp32_unpruned"]["value"]
+        line["bf16_over_fp32_note"] = ("the BF16 precision form (pruned, FP64 ranking) over the plain FP32 "
+                                       "form without pruning; over this line's pruned FP32 value: %.3f"
+                                       % (f["bf16_tc"]["value"] / value))
+        u = f["fp32_unpruned"]
+        line["roofline"]["unpruned"] = {
+            "kernel": "csx::screen_q_kernel<true>", "kernel_ms_per_launch": u["screen_kernel_ms"],
+            "algorithmic_ops_per_candidate": LANE_OPS_PER_CAND,
+            "issue_slots": issue_slots(args.lam / (u["screen_kernel_ms"] * 1e-3) * LANE_OPS_PER_CAND / 1e12,
+                                       clocks)}
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args, args.cpu_seconds)
     print(json.dumps(line), flush=True)
