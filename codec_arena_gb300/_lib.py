@@ -108,6 +108,9 @@ SIGNATURES = {
     "csx_screen_range": (ctypes.c_int, [ctypes.POINTER(CsxCfg), ctypes.POINTER(CsxModel), ctypes.c_void_p,
                                         ctypes.c_int, _u64, _u64, ctypes.c_void_p, _u64, ctypes.POINTER(_u64),
                                         ctypes.POINTER(_u64)]),
+    "csx_screen_items": (ctypes.c_int, [ctypes.POINTER(CsxCfg), ctypes.POINTER(CsxModel), ctypes.c_void_p,
+                                        ctypes.c_int, _u32, _u32, ctypes.c_void_p, _u64, ctypes.POINTER(_u64),
+                                        ctypes.POINTER(_u64)]),
     "csx_screen_device": (ctypes.c_int, [ctypes.POINTER(CsxCfg), ctypes.POINTER(CsxModel),
                                          ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, _u64,
                                          ctypes.c_void_p, ctypes.c_void_p]),

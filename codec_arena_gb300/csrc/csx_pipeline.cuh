@@ -68,6 +68,8 @@ struct Ctrl {
     unsigned long long screened;
     unsigned long long n_out;
     unsigned long long exact_evals;  // reference-order evaluations (filter mode)
+    unsigned int item_begin;         // first item of this call's share (item sharding), else 0
+    unsigned int pad_;
 };
 
 // Streams of one screen: T in all (src/screen.zig:267), of which this call
@@ -633,6 +635,18 @@ __global__ void emit_kernel(StreamGeom g, const SegOut *__restrict__ outs, const
 }
 
 // Streams no longer than one item: one item per stream, starting at draw 0.
+// Item sharding: this call screens items [n * shard / n_shards, n * (shard +
+// 1) / n_shards) of the n the item stages emitted (the screen kernels pull
+// items from next_item up to n_items).
+__global__ void shard_items_kernel(Ctrl *ctrl, uint32_t shard, uint32_t n_shards) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        const uint64_t n = ctrl->n_items;
+        ctrl->item_begin = static_cast<unsigned int>(n * shard / n_shards);
+        ctrl->next_item = ctrl->item_begin;
+        ctrl->n_items = static_cast<unsigned int>(n * (shard + 1) / n_shards);
+    }
+}
+
 __global__ void stream_items_kernel(StreamGeom g, Item *__restrict__ items, Ctrl *__restrict__ ctrl) {
     const uint64_t tl = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (tl == 0) ctrl->n_items = static_cast<unsigned int>(g.nT);

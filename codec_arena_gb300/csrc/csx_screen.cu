@@ -303,11 +303,21 @@ void segment_geometry(const csx_cfg &cfg, uint64_t seg, uint64_t ck_mult, Stream
     g.ckcap = static_cast<uint32_t>((ck_mult * L / 33) / (1ull << g.d_log2) + 3);
 }
 
+// A share of one generation's work items (csx_screen_items): every share
+// builds the same item list and screens its part of it.
+struct Shard {
+    uint32_t index = 0, count = 1;
+};
+
 // grid_override, item_cands, seg_cands: 0 = automatic (the batched screen
-// passes its own grid and the tuner's sizes).
+// passes its own grid and the tuner's sizes). A sharded call sizes its items
+// by a fixed SM count, so that every share's item list is the same whatever
+// GPU it runs on.
+constexpr int kItemRefSms = 152;
+
 int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int ne, Plan *pl,
               int grid_override = 0, uint64_t item_cands = 0, uint64_t seg_cands = 0, uint64_t t_begin = 0,
-              uint64_t t_end = 0, const csx_model_full *full = nullptr) {
+              uint64_t t_end = 0, const csx_model_full *full = nullptr, bool sharded = false) {
     StreamGeom &g = pl->g;
     int src = split_streams(cfg, t_begin, t_end, g);
     if (src) return src;
@@ -367,7 +377,7 @@ int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int
     // 0.25% with the filter kernel's two)
     uint64_t d = item_cands ? item_cands : env_u64("CSX_ITEM_CANDS", 0);
     if (d == 0) {
-        const uint64_t target = 64ull * 3 * static_cast<uint64_t>(cx.num_sms) * kThreads;
+        const uint64_t target = 64ull * 3 * static_cast<uint64_t>(sharded ? kItemRefSms : cx.num_sms) * kThreads;
         d = std::max<uint64_t>(1, lam_range / target);
         d = std::min<uint64_t>(16384, std::max<uint64_t>(64, d));
     }
@@ -478,9 +488,10 @@ int enqueue_merge(Entry *cur, Entry *nxt, uint32_t nl, uint32_t kpad, cudaStream
 // Enqueue the whole pipeline on `st`. Device inputs: genomes (csx_genome x ne).
 int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, const csx_genome *d_genomes,
                    int ne, csx_survivor *d_out, unsigned long long *d_result, cudaStream_t st,
-                   uint64_t t_begin = 0, uint64_t t_end = 0, const csx_model_full *full = nullptr) {
+                   uint64_t t_begin = 0, uint64_t t_end = 0, const csx_model_full *full = nullptr,
+                   Shard shard = Shard{}) {
     Plan pl;
-    int rc = make_plan(cx, cfg, model, ne, &pl, 0, 0, 0, t_begin, t_end, full);
+    int rc = make_plan(cx, cfg, model, ne, &pl, 0, 0, 0, t_begin, t_end, full, shard.count > 1);
     if (rc) return rc;
     const StreamGeom &g = pl.g;
     const bool fast = pl.fast_delta;
@@ -530,6 +541,11 @@ int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, cons
                        static_cast<SegOut *>(cx.segout.p), static_cast<uint32_t *>(cx.off.p), items, ctrl, st,
                        &launches);
     if (rc) return rc;
+    if (shard.count > 1) {
+        shard_items_kernel<<<1, 32, 0, st>>>(ctrl, shard.index, shard.count);
+        CSX_CUDA(cudaGetLastError());
+        ++launches;
+    }
     CSX_CUDA(mark(2));
 
     const ScreenArgs A = screen_args(cfg, model, sc, pl, tab, items, ctrl, static_cast<Entry *>(cx.lists_a.p));
@@ -711,7 +727,7 @@ namespace csx {
 // csx_screen / csx_screen_range: host buffers, a private stream, synchronous.
 int screen_host(const csx_cfg *cfg, const csx_model *model, const csx_genome *elites, int n_elites,
                 uint64_t t_begin, uint64_t t_end, csx_survivor *out, uint64_t out_cap, uint64_t *n_out,
-                uint64_t *screened, const csx_model_full *full = nullptr) {
+                uint64_t *screened, const csx_model_full *full = nullptr, Shard shard = Shard{}) {
     if (n_out) *n_out = 0;
     if (screened) *screened = 0;
     int rc = check_common(cfg, model, n_elites);
@@ -740,7 +756,7 @@ int screen_host(const csx_cfg *cfg, const csx_model *model, const csx_genome *el
     cudaError_t e = cudaMemcpyAsync(dg, elites, static_cast<size_t>(n_elites) * sizeof(csx_genome),
                                     cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) {
-        rc = enqueue_screen(*cx, *cfg, *model, dg, n_elites, ds, dr, st, t_begin, t_end, full);
+        rc = enqueue_screen(*cx, *cfg, *model, dg, n_elites, ds, dr, st, t_begin, t_end, full, shard);
         if (rc == CSX_OK) {
             e = cudaMemcpyAsync(res, dr, sizeof(res), cudaMemcpyDeviceToHost, st);
             if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -797,6 +813,20 @@ int csx_screen_full_range(const csx_cfg *cfg, const csx_model_full *model, const
     return screen_host(cfg, &kZeroModel, elites, n_elites, t_begin, t_end, out, out_cap, n_out, screened, model);
 }
 
+int csx_screen_items(const csx_cfg *cfg, const csx_model *model, const csx_genome *elites, int n_elites,
+                     uint32_t shard, uint32_t n_shards, csx_survivor *out, uint64_t out_cap, uint64_t *n_out,
+                     uint64_t *screened) {
+    if (n_shards == 0 || shard >= n_shards) {
+        if (n_out) *n_out = 0;
+        if (screened) *screened = 0;
+        return CSX_ERR_BAD_ARGS;
+    }
+    Shard sh;
+    sh.index = shard;
+    sh.count = n_shards;
+    return screen_host(cfg, model, elites, n_elites, 0, 0, out, out_cap, n_out, screened, nullptr, sh);
+}
+
 int csx_screen_range(const csx_cfg *cfg, const csx_model *model, const csx_genome *elites, int n_elites,
                      uint64_t t_begin, uint64_t t_end, csx_survivor *out, uint64_t out_cap, uint64_t *n_out,
                      uint64_t *screened) {
@@ -834,6 +864,8 @@ static NoAllocDevice g_noalloc[64];
 
 // Once per device, with that device current: the scratch's device address.
 // In host code g_noalloc_scratch names a host-side stand-in, never passed on.
+// The address is kept for the life of the process: a cudaDeviceReset, which
+// unloads this library's device code, is not supported between calls.
 int noalloc_setup(int dev, NoAllocDevice **out) {
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
     NoAllocDevice &d = g_noalloc[dev];
@@ -854,6 +886,12 @@ int noalloc_setup(int dev, NoAllocDevice **out) {
 // Plan for the fixed scratch: items of at least 16384 candidates (fewer items
 // and checkpoints). A segment's range of cnt candidates holds at most
 // ceil(cnt / D) split points, so items <= 2 * segments + lambda / D.
+// Checkpoints are sized for one segment's chain (ck_mult 1, where the pooled
+// plan takes 2): a link can land past its segment, and a checkpoint the walk
+// cannot store is dropped; split_range then clamps at the last stored one, so
+// that segment's last item grows instead (still within the items bound above)
+// and the result is unchanged. The pooled plan's margin buys smaller items,
+// which this plan does not need.
 int plan_noalloc(const NoAllocDevice &dv, const csx_cfg &cfg, const csx_model &model, int ne, Plan *pl) {
     StreamGeom &g = pl->g;
     int src = split_streams(cfg, 0, 0, g);

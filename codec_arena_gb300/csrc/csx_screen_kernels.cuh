@@ -468,7 +468,7 @@ __global__ void result_kernel(const Ctrl *__restrict__ ctrl, unsigned long long 
         result[0] = ctrl->n_out;
         result[1] = ctrl->screened;
         result[2] = ctrl->err;
-        result[3] = ctrl->n_items;
+        result[3] = ctrl->n_items - ctrl->item_begin;
     }
 }
 

@@ -29,7 +29,10 @@ def island_seed(seed: int, shard: int, gen: int = 0) -> int:
 
 def stream_ranges(threads: int, lam: int, world: int) -> List[range]:
     """Split the T = max(1, min(threads, lambda)) streams of one generation
-    into `world` contiguous ranges (src/screen.zig:267)."""
+    into `world` contiguous ranges (src/screen.zig:267). With more ranks than
+    streams the last ranks get empty ranges (screen.screen returns no
+    survivors for them, so they still join the gather); item_shard splits a
+    generation over any number of ranks instead."""
     T = max(1, min(int(threads), int(lam)))
     base, extra = divmod(T, world)
     out, t0 = [], 0
@@ -38,6 +41,12 @@ def stream_ranges(threads: int, lam: int, world: int) -> List[range]:
         out.append(range(t0, t0 + n))
         t0 += n
     return out
+
+
+def item_shard(rank: int, world: int):
+    """The items= argument of screen.screen for one rank's share of a
+    generation's work items (csx_screen_items)."""
+    return (int(rank), int(world))
 
 
 def merge_survivors(parts: Iterable[np.ndarray], keep: int) -> np.ndarray:
@@ -86,4 +95,4 @@ def gather_survivors(local: np.ndarray, keep: int, device=None) -> np.ndarray:
     return merge_survivors(parts, keep)
 
 
-__all__ = ["island_seed", "stream_ranges", "merge_survivors", "max_over_ranks", "gather_survivors"]
+__all__ = ["island_seed", "stream_ranges", "item_shard", "merge_survivors", "max_over_ranks", "gather_survivors"]

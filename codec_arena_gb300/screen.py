@@ -131,19 +131,32 @@ def _elites_array(elites) -> np.ndarray:
     return e
 
 
-def screen(cfg: Cfg, model: Model, elites, streams: Optional[Tuple[int, int]] = None) -> Tuple[np.ndarray, int]:
+def screen(cfg: Cfg, model: Model, elites, streams: Optional[Tuple[int, int]] = None,
+           items: Optional[Tuple[int, int]] = None) -> Tuple[np.ndarray, int]:
     """run() without the file output: (survivors sorted by score desc, screened).
 
     streams=(a, b) screens only RNG streams a..b-1 of the generation (one
-    rank's share when a generation is sharded by stream; merge the ranks'
-    survivors with parallel.merge_survivors). A ModelFull scores the
-    candidates on the full 29-gene quadratic surface instead."""
+    rank's share when a generation is sharded by stream; an empty range gives
+    no survivors and screens nothing). items=(r, W) screens share r of W of
+    the generation's work items (any number of ranks, even more than
+    streams). Merge the ranks' survivors with parallel.merge_survivors. A
+    ModelFull scores the candidates on the full 29-gene quadratic surface
+    instead (stream ranges only)."""
     e = _elites_array(elites)
     keep_n = min(int(cfg.keep), int(cfg.lambda_))
     out = np.zeros(max(keep_n, 1), dtype=SURVIVOR_DTYPE)
     n_out = ctypes.c_uint64(0)
     screened = ctypes.c_uint64(0)
     c = cfg.c()
+    if streams is not None and int(streams[0]) == int(streams[1]):
+        return out[:0], 0  # a rank with no stream of its own (more ranks than streams)
+    if items is not None:
+        if isinstance(model, ModelFull) or streams is not None:
+            raise ValueError("items= shards the reference surface's whole generation")
+        check(lib().csx_screen_items(ctypes.byref(c), ctypes.byref(model.c), e.ctypes.data, int(e.shape[0]),
+                                     int(items[0]), int(items[1]), out.ctypes.data, keep_n, ctypes.byref(n_out),
+                                     ctypes.byref(screened)), "screen_items")
+        return out[: n_out.value], int(screened.value)
     if isinstance(model, ModelFull) and streams is None:
         check(lib().csx_screen_full(ctypes.byref(c), ctypes.byref(model.c), e.ctypes.data, int(e.shape[0]),
                                     out.ctypes.data, keep_n, ctypes.byref(n_out), ctypes.byref(screened)),

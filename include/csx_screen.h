@@ -55,12 +55,15 @@ enum {
 #define CSX_FLAG_EXACT_ALL 0x8u    /* score every candidate in the reference's f32 order
                                       instead of filtering with a certified fast score */
 #define CSX_FLAG_STAGE_TIMES 0x10u /* record per-stage device times (csx_last_run_info) */
-#define CSX_FLAG_TC_BF16 0x20u     /* precision form: quadratic block on the tensor cores in BF16;
-                                      candidates within max(1e-3 relative, the form's certified
-                                      error bound) of the K-th score are rescored in FP64 and the
-                                      survivors ranked by that FP64 score (rounded to f32): the
-                                      FP64 top-K, genes bit-exact. csx_screen / csx_screen_device */
-#define CSX_FLAG_TC_FP16 0x40u     /* the same in FP16 with x' = 2g - 1 */
+#define CSX_FLAG_TC_BF16 0x20u     /* precision form: survivors ranked by their FP64 score (rounded
+                                      to f32): the FP64 top-K, genes bit-exact. By default the
+                                      pruning bound runs on BF16 tensor cores and the candidates it
+                                      cannot rule out are filtered by FFMA and scored in FP64; with
+                                      CSX_FLAG_NO_PRUNE the quadratic block of every candidate runs
+                                      on the tensor cores and candidates within max(1e-3 relative,
+                                      the form's certified error bound) of the K-th score are
+                                      rescored in FP64. csx_screen / csx_screen_device */
+#define CSX_FLAG_TC_FP16 0x40u     /* the same with FP16 tiles (unpruned: x' = 2g - 1) */
 #define CSX_FLAG_NO_PRUNE 0x80u    /* score every candidate's full synthesis (the filter form)
                                       instead of skipping, by a certified bound taken after the
                                       crossover bits, candidates that cannot reach the top-K.
@@ -160,6 +163,21 @@ int csx_screen_range(const csx_cfg *cfg, const csx_model *model, const csx_genom
                      uint64_t t_begin, uint64_t t_end, csx_survivor *out, uint64_t out_cap, uint64_t *n_out,
                      uint64_t *screened);
 
+/* csx_screen restricted to one share of the generation's work items: the
+ * items (runs of consecutive candidates of one stream, built from the
+ * configuration alone, whatever GPU runs the call) are cut into n_shards
+ * contiguous parts and this call screens part `shard` (0 <= shard <
+ * n_shards). Survivors carry their global stream and index; the top-K of all
+ * shards' survivors in the order score descending, (stream, index)
+ * ascending equals csx_screen's result, and the shards' *screened sum to
+ * lambda. This splits one generation over any number of ranks, even more
+ * ranks than RNG streams (csx_screen_range splits by stream). A share may be
+ * empty. No reference counterpart (the reference runs every stream in one
+ * process). */
+int csx_screen_items(const csx_cfg *cfg, const csx_model *model, const csx_genome *elites, int n_elites,
+                     uint32_t shard, uint32_t n_shards, csx_survivor *out, uint64_t out_cap, uint64_t *n_out,
+                     uint64_t *screened);
+
 /* Same, with device-resident elites and survivors, enqueued on `cuda_stream`
  * (a cudaStream_t; NULL = the legacy default stream). d_result receives four
  * device uint64: survivor count, screened count, device error bits (0 = ok)
@@ -180,7 +198,12 @@ int csx_screen_device(const csx_cfg *cfg, const csx_model *model, const csx_geno
  * generation needs about 14 MiB). The first call on a device looks up the
  * array's device address; make that first call before any stream capture.
  * All calls share the array: calls that overlap on the GPU race, so order
- * them (one stream, or events). Results equal csx_screen_device's. */
+ * them (one stream, or events). Results equal csx_screen_device's for the
+ * reference surface. Not offered here: the precision-form flags
+ * (CSX_FLAG_TC_BF16 / TC_FP16 return CSX_ERR_BAD_ARGS), the full surface, and
+ * csx_last_run_info (not updated by this call). The device address of the
+ * array is looked up on the first call and kept: a cudaDeviceReset between
+ * calls is not supported. */
 int csx_screen_device_noalloc(const csx_cfg *cfg, const csx_model *model, const csx_genome *d_elites,
                               int n_elites, csx_survivor *d_out, uint64_t out_cap, uint64_t *d_result,
                               void *cuda_stream);

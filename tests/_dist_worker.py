@@ -2,7 +2,8 @@
 the gloo backend. Each rank screens its share of one generation's RNG streams
 -- with the GPU engine (csx_screen_range) when the sixth argument is "gpu",
 else with the CPU oracle -- then the ranks merge survivors over gloo and agree
-on the slowest rank's time."""
+on the slowest rank's time. With "items" each rank screens its share of the
+generation's work items instead (csx_screen_items)."""
 import json
 import os
 import sys
@@ -28,7 +29,12 @@ def main():
     el = wl.seeded_elites(16, seed=3)
     t0 = time.perf_counter()
     rg = parallel.stream_ranges(T, lam, world)[rank]
-    if engine == "gpu":
+    if engine == "items":  # this rank's share of the generation's work items (csx_screen_items)
+        from codec_arena_gb300 import screen
+
+        mine, _ = screen.screen(screen.Cfg(lam, keep, seed, threads=T), screen.Model.from_compact(wl.surrogate_161()),
+                                el, items=parallel.item_shard(rank, world))
+    elif engine == "gpu":
         from codec_arena_gb300 import screen
 
         mine, _ = screen.screen(screen.Cfg(lam, keep, seed, threads=T), screen.Model.from_compact(wl.surrogate_161()),

@@ -373,14 +373,39 @@ def test_stream_ranges_merge_to_the_generation(lam, T, parts):
     assert parallel.merge_survivors([p[0] for p in pieces], 128).tobytes() == full.tobytes()
 
 
+@pytest.mark.parametrize("lam,T,W", [(30_000_000, 4, 2), (30_000_000, 4, 7), (5_000_003, 2, 3), (1_000, 3, 5),
+                                     (20, 4, 9)])
+def test_item_shards_merge_to_the_generation(lam, T, W):
+    """csx_screen_items: W shares of the generation's work items (W may exceed
+    the stream count and the item count), merged in the reference's order,
+    equal the whole generation bit for bit; the shares' screened counts sum
+    to lambda."""
+    from codec_arena_gb300 import parallel, screen, workloads as wl
+
+    el = wl.seeded_elites(64)
+    m = screen.Model.from_compact(wl.surrogate_161())
+    cfg = screen.Cfg(lam, 128, 31, threads=T)
+    full, n = screen.screen(cfg, m, el)
+    pieces = [screen.screen(cfg, m, el, items=parallel.item_shard(r, W)) for r in range(W)]
+    assert sum(p[1] for p in pieces) == n == lam
+    assert parallel.merge_survivors([p[0] for p in pieces], 128).tobytes() == full.tobytes()
+
+
 def test_stream_range_errors():
     from codec_arena_gb300 import _lib, screen, workloads as wl
 
     m = screen.Model.from_compact(wl.surrogate_161())
     el = wl.seeded_elites(8)
-    for rg in [(2, 2), (3, 1), (0, 5)]:
+    for rg in [(3, 1), (0, 5)]:
         with pytest.raises(_lib.CsxError) as e:
             screen.screen(screen.Cfg(1000, 8, 1, threads=4), m, el, streams=rg)
+        assert e.value.status == _lib.ERR_BAD_ARGS
+    # an empty range (a rank with no stream of its own) screens nothing
+    surv, n = screen.screen(screen.Cfg(1000, 8, 1, threads=4), m, el, streams=(2, 2))
+    assert len(surv) == 0 and n == 0
+    for sh in [(0, 0), (3, 3)]:
+        with pytest.raises(_lib.CsxError) as e:
+            screen.screen(screen.Cfg(1000, 8, 1, threads=4), m, el, items=sh)
         assert e.value.status == _lib.ERR_BAD_ARGS
 
 

@@ -49,9 +49,9 @@ def test_merge_equals_single_process(orc):
     assert parallel.merge_survivors(parts, keep).tobytes() == full.tobytes()
 
 
-def _run_world_2(tmp_path, lam, keep, seed, T, engine, port):
+def _run_world_2(tmp_path, lam, keep, seed, T, engine, port, nproc=2):
     out = tmp_path / f"rank0_{engine}.json"
-    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=2",
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={nproc}",
            "--master-addr=127.0.0.1", f"--master-port={port}",
            os.path.join(ROOT, "tests", "_dist_worker.py"), str(lam), str(keep), str(seed), str(T), str(out), engine]
     env = dict(os.environ, OMP_NUM_THREADS="1")
@@ -97,3 +97,39 @@ def test_gloo_world_size_2(orc, tmp_path):
     full, _ = orc.screen(orc.cfg(lam, keep, seed, threads=T), orc.model_from_compact(wl.surrogate_161()),
                          wl.seeded_elites(16, seed=3))
     assert merged.tobytes() == full.tobytes()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("engine,nproc,T,port", [("items", 2, 4, 29541), ("items", 3, 2, 29542),
+                                                 ("gpu", 3, 2, 29543)])
+def test_gloo_split_one_generation_gpu(orc, tmp_path, engine, nproc, T, port):
+    """One generation split over gloo ranks on the GPU: by work items (two
+    ranks at T = 4; three ranks at T = 2, more ranks than streams) and by
+    streams with three ranks at T = 2 (one rank has no stream and joins the
+    gather empty). The merged survivors equal the oracle's single-process
+    generation."""
+    from conftest import has_gpu
+
+    if not has_gpu():
+        pytest.skip("no CUDA device")
+    from codec_arena_gb300 import _lib, workloads as wl
+
+    lam, keep, seed = 2_000_003, 48, 13
+    res = _run_world_2(tmp_path, lam, keep, seed, T, engine, port, nproc=nproc)
+    merged = np.frombuffer(bytes.fromhex(res["merged"]), dtype=_lib.SURVIVOR_DTYPE)
+    full, _ = orc.screen(orc.cfg(lam, keep, seed, threads=T), orc.model_from_compact(wl.surrogate_161()),
+                         wl.seeded_elites(16, seed=3))
+    assert merged.tobytes() == full.tobytes()
+
+
+def test_gloo_more_ranks_than_streams_oracle(orc, tmp_path):
+    """Three ranks at T = 2 with the oracle engine: the rank without a stream
+    gathers an empty list and the merge equals the generation."""
+    from codec_arena_gb300 import _lib, workloads as wl
+
+    lam, keep, seed, T = 9_000, 30, 2, 2
+    res = _run_world_2(tmp_path, lam, keep, seed, T, "oracle", 29544, nproc=3)
+    merged = np.frombuffer(bytes.fromhex(res["merged"]), dtype=_lib.SURVIVOR_DTYPE)
+    full, _ = orc.screen(orc.cfg(lam, keep, seed, threads=T), orc.model_from_compact(wl.surrogate_161()),
+                         wl.seeded_elites(16, seed=3))
+    assert res["world"] == 3 and merged.tobytes() == full.tobytes()
