@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(kThreads, 3) screen_batch_kernel(const __grid_
             const unsigned long long k1 =
                 (static_cast<unsigned long long>(score_okey(s)) << 32) | static_cast<unsigned int>(~q.item);
             const unsigned long long k2 = (static_cast<unsigned long long>(~q.dcand) << 32) | q.ddraw;
-            if (k1 > t1 || (k1 == t1 && k2 > t2)) E[s_kpad + atomicAdd(&s_buf_n, 1u)] = Entry{k1, k2};
+            E[s_kpad + atomicAdd(&s_buf_n, 1u)] = Entry{k1, k2};  // score >= ts: ties with the K-th kept
         }
     };
 
@@ -280,18 +280,16 @@ __global__ void __launch_bounds__(kThreads, 3) screen_batch_kernel(const __grid_
             } else {
                 s = synth_score<kFastDelta, false>(s_m, s_sc, el, seed_t, p, h, nullptr);
             }
-            if (!kFilter && s >= ts) {
+            if (!kFilter && s >= ts) {  // ties with the running K-th score enter too
                 const unsigned long long k1 =
                     (static_cast<unsigned long long>(score_okey(s)) << 32) | static_cast<unsigned int>(~item);
                 const unsigned long long k2 = (static_cast<unsigned long long>(~dcand) << 32) | ddraw;
-                if (k1 > t1 || (k1 == t1 && k2 > t2)) {
-                    const unsigned int slot = atomicAdd(&s_buf_n, 1u);
-                    if (slot < bcap) {
-                        buf[slot] = Entry{k1, k2};
-                    } else {
-                        has_def = true;
-                        def = Entry{k1, k2};
-                    }
+                const unsigned int slot = atomicAdd(&s_buf_n, 1u);
+                if (slot < bcap) {
+                    buf[slot] = Entry{k1, k2};
+                } else {
+                    has_def = true;
+                    def = Entry{k1, k2};
                 }
             }
             p += h.len;
@@ -731,6 +729,24 @@ int csx_screen_batch(int n_islands, const csx_cfg *cfgs, const csx_model *models
         off += cfgs[i].keep;
     }
     CSX_CUDA(cudaStreamSynchronize(st));
+    // exact ties as the reference's per-stream heaps order them (fix_ties);
+    // the merge tree leaves each island's final list in lists_b after an odd
+    // number of levels
+    bool in_b = false;
+    for (uint32_t nl = static_cast<uint32_t>(L.grid); nl > 1; nl = (nl + 1) / 2) in_b = !in_b;
+    off = 0;
+    for (int i = 0; i < n_islands && !bad; ++i) {
+        const uint64_t cnt = std::min<uint64_t>(res[4 * i], std::min<uint64_t>(cfgs[i].keep, cfgs[i].lambda));
+        if (cnt > 0 && !(cfgs[i].flags & CSX_FLAG_AS_SHIPPED)) {
+            const IslandBufs &b = L.b[i];
+            rc = fix_ties(*cx, cfgs[i], models[i], nullptr, n_elites[i], 0, 0, out + off, cnt,
+                          ScreenBufs{b.tab, b.items, res[4 * i + 3], b.ids, b.tribes, in_b ? b.lb : b.la,
+                                     L.pl[i].kpad},
+                          st);
+            if (rc) return rc;
+        }
+        off += cfgs[i].keep;
+    }
     CSX_CUDA(cudaEventRecord(cx->done, st));
     cx->binfo = csx_batch_info{};
     cx->binfo.islands = static_cast<uint32_t>(n_islands);

@@ -77,6 +77,7 @@ struct Ctrl {
 // caller shards a generation by stream). Segment s is local to the range.
 struct StreamGeom {
     uint64_t seed, T, per, my_last, L, n_seg, t0, nT;
+    uint64_t link_cap;  // link steps before a boundary is declared failed (kLinkCap; CSX_LINK_CAP)
     uint32_t C, C_last, d_log2, ckcap;
 };
 
@@ -303,7 +304,7 @@ __global__ void link_kernel(SynthConst sc, StreamGeom g, SegRec *__restrict__ re
                 kb = static_cast<uint64_t>(cm) << g.d_log2;
                 break;
             }
-            if (steps > kLinkCap) {
+            if (steps > g.link_cap) {
                 fail = true;
                 break;
             }
@@ -349,7 +350,7 @@ __global__ void link_kernel(SynthConst sc, StreamGeom g, SegRec *__restrict__ re
         x = nx;
         y = ny;
         steps += adv_x + adv_y;
-        if (steps > kLinkCap) {
+        if (steps > g.link_cap) {
             fail = true;
             break;
         }
@@ -594,6 +595,9 @@ __global__ void __launch_bounds__(1024) scan_kernel(const SegOut *__restrict__ o
             atomicOr(&ctrl->err, kErrItems);
             base = 0;
         }
+        // after a failed link or assembly no item is emitted or screened: the
+        // stages that follow see n_items = 0 and the error bits void the call
+        if (ctrl->err) base = 0;
         ctrl->n_items = static_cast<unsigned int>(base);
     }
 }
@@ -604,7 +608,7 @@ __global__ void emit_kernel(StreamGeom g, const SegOut *__restrict__ outs, const
     const uint64_t s = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (s >= g.n_seg) return;
     const SegOut o = outs[s];
-    if (o.cnt == 0 || (ctrl->err & kErrItems)) return;
+    if (o.cnt == 0 || ctrl->err) return;
     uint64_t t;
     uint32_t c;
     seg_of(g, s, t, c);

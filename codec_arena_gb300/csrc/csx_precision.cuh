@@ -123,6 +123,9 @@ __global__ void __launch_bounds__(128) tc_score_kernel(const __grid_constant__ T
     g.phase = 0;
     g.issuer = tid == 0;
     bool ok = true;
+    __shared__ uint32_t s_gbad, s_fail_phase;
+    if (tid == 0) s_gbad = s_fail_phase = 0;
+    __syncthreads();
     for (int64_t r0 = static_cast<int64_t>(blockIdx.x) * 128; r0 < n; r0 += static_cast<int64_t>(gridDim.x) * 128) {
         const int64_t r = r0 + tid;
         float x[16];
@@ -137,13 +140,15 @@ __global__ void __launch_bounds__(128) tc_score_kernel(const __grid_constant__ T
 #pragma unroll
         for (int j = 0; j < 8; ++j) pk[j] = pack2(x[2 * j], x[2 * j + 1], kFp16);
         float y[16];
-        ok = tc_round(g, pk, tid, y) && ok;
+        if (!tcp_round(g, pk, tid, y, &s_gbad, &s_fail_phase)) ok = false;  // a give-up stops the MMAs
         float s = R;
 #pragma unroll
         for (int i = 0; i < 16; ++i) s = __fmaf_rn(x[i], y[i], s);
         if (r < n) out[r] = s;
     }
     if (!ok) atomicOr(err, kErrTc);
+    __syncthreads();
+    if (s_gbad != 0u && g.issuer) (void)mbar_wait(g.mbar, s_fail_phase);  // bounded: the MMA given up on
     tc_fence_before();
     __syncthreads();
     tc_fence_after();

@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(kThreads, 2) screen_p_kernel(const __grid_cons
             const unsigned long long k1 =
                 (static_cast<unsigned long long>(score_okey(s)) << 32) | static_cast<unsigned int>(~q.item);
             const unsigned long long k2 = (static_cast<unsigned long long>(~q.dcand) << 32) | q.ddraw;
-            if (k1 > t1 || (k1 == t1 && k2 > t2)) buf[atomicAdd(&s_buf_n, 1u)] = Entry{k1, k2};
+            buf[atomicAdd(&s_buf_n, 1u)] = Entry{k1, k2};  // score >= ts: ties with the K-th kept
         }
     };
 
@@ -383,49 +383,6 @@ __device__ __forceinline__ void prune_parents(const PruneArgs &A, const float *_
     }
 }
 
-// One tensor-core round of a 128-thread group (tc_round of csx_tc.cuh with a
-// give-up path that keeps the group in step). gbad is the group's flag in
-// shared memory, written only by the group's threads, after their wait of a
-// round and before the next round's barrier: every thread of the group reads
-// the same value after that barrier, so once a wait has given up the whole
-// group skips the MMA and the wait from the next round on, and every thread
-// still passes the same barriers. *fail_phase receives the parity of the
-// wait that gave up. Returns false when this thread's wait gave up.
-__device__ __forceinline__ bool tcp_round(TcGroup &g, const uint32_t (&pk)[8], uint32_t row, float (&y)[16],
-                                          volatile uint32_t *gbad, volatile uint32_t *fail_phase) {
-    const uint32_t a = g.xs + (row >> 3) * 256u + (row & 7u) * 16u;
-    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(a), "r"(pk[0]), "r"(pk[1]), "r"(pk[2]), "r"(pk[3])
-                 : "memory");
-    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(a + 128u), "r"(pk[4]), "r"(pk[5]), "r"(pk[6]),
-                 "r"(pk[7])
-                 : "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    tc_fence_before();
-    if (g.bar_id == 1)
-        asm volatile("bar.sync 1, 128;" ::: "memory");
-    else
-        asm volatile("bar.sync 2, 128;" ::: "memory");
-    if (*gbad != 0u) {
-#pragma unroll
-        for (int i = 0; i < 16; ++i) y[i] = 0.0f;
-        return true;
-    }
-    if (g.issuer) {
-        tc_fence_after();
-        tc_mma(g.tmem_d, g.adesc, g.bdesc, g.idesc);
-        tc_commit(g.mbar);
-    }
-    const bool ok = mbar_wait(g.mbar, g.phase);
-    if (!ok) {
-        *fail_phase = g.phase;
-        *gbad = 1u;
-    }
-    g.phase ^= 1u;
-    tc_fence_after();
-    tc_ld16(g.tmem_ld, y);
-    return ok;
-}
-
 // The pruning screen with the bound's gradient on the tensor cores. Each
 // 128-thread group runs rounds in step: every thread puts its candidate's
 // parent genes (FP16) in row tid % 128 of the group's X tile (a zero row when
@@ -525,7 +482,7 @@ __global__ void __launch_bounds__(kThreads, 3) screen_pt_kernel(const __grid_con
             const unsigned long long k1 =
                 (static_cast<unsigned long long>(score_okey(s)) << 32) | static_cast<unsigned int>(~q.item);
             const unsigned long long k2 = (static_cast<unsigned long long>(~q.dcand) << 32) | q.ddraw;
-            if (k1 > t1 || (k1 == t1 && k2 > t2)) buf[atomicAdd(&s_buf_n, 1u)] = Entry{k1, k2};
+            buf[atomicAdd(&s_buf_n, 1u)] = Entry{k1, k2};  // score >= ts: ties with the K-th kept
         }
     };
 

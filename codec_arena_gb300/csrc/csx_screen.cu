@@ -43,7 +43,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <set>
 #include <vector>
 
 #include "../../include/csx_screen.h"
@@ -52,6 +54,7 @@
 #include "csx_pipeline.cuh"
 #include "csx_screen_kernels.cuh"
 #include "csx_prune.cuh"
+#include "csx_ties.cuh"
 
 namespace csx {
 
@@ -82,7 +85,7 @@ struct Context {
     bool timed = false;
     csx_run_info info{};
     DevBuf genomes, tab, ids, tribes, recs, ck, segout, off, items, lists_a, lists_b, ctrl, surv,
-        result, pub;
+        result, pub, tie_hits, tie_count, tie_streams, tie_out;
     // batched islands
     DevBuf batch, b_genomes, b_surv, b_result;
     void *pinned = nullptr;         // host staging of the island descriptors (page-locked)
@@ -93,6 +96,8 @@ struct Context {
     cudaStream_t pst = nullptr;     // private stream of the host batch call
     cudaGraphExec_t gexec = nullptr;
     csx_batch_info binfo{};
+    const Entry *fin = nullptr;  // final list of the last single screen (kpad entries)
+    uint32_t fin_kpad = 0;
 };
 
 Context g_ctx[64];
@@ -252,6 +257,7 @@ int split_streams(const csx_cfg &cfg, uint64_t t_begin, uint64_t t_end, StreamGe
     g.per = cfg.lambda / g.T;
     g.my_last = cfg.lambda - (g.T - 1) * g.per;
     if (g.T >= 0xFFFFFFFFull) return CSX_ERR_LIMIT;
+    g.link_cap = env_u64("CSX_LINK_CAP", kLinkCap);  // a lower cap makes the link's failure path testable
     if (t_end == 0) t_end = g.T;  // the whole generation
     if (t_begin >= t_end || t_end > g.T) return CSX_ERR_BAD_ARGS;
     g.t0 = t_begin;
@@ -278,7 +284,10 @@ void screen_shape(const csx_cfg &cfg, const csx_model &model, bool full, Plan *p
     pl->prune_tc = pl->prune && (tcf != 0 || !(cfg.flags & CSX_FLAG_PRUNE_FFMA)) &&
                    make_prune_tc(model, pl->pc, tcf != CSX_FLAG_TC_BF16, &pl->ptc);
     if (tcf && !pl->prune_tc) pl->prune = false;
-    pl->kpad = std::max<uint32_t>(32, pow2_at_least(cfg.keep));
+    // the lists keep K + 1 entries where that fits (keep <= 2048): the final
+    // (K+1)-th entry tells whether a candidate outside the survivors ties with
+    // the K-th score (exact-tie order, fix_ties)
+    pl->kpad = std::max<uint32_t>(32, pow2_at_least(cfg.keep + (cfg.keep <= 2048 ? 1 : 0)));
     pl->sort_n = pow2_at_least(pl->kpad + 4ull * kThreads);
     pl->buf_cap = pl->sort_n - pl->kpad;
 }
@@ -353,7 +362,10 @@ int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int
         // TMEM (32 columns each) hold three, which run 9% faster than two
         // (measured). The screen is persistent with dynamic work, so any grid
         // is correct.
-        if (pl->prune_tc) pl->grid = std::max(pl->grid, 3 * cx.num_sms);
+        if (pl->prune_tc) {
+            const int fit = static_cast<int>((228u << 10) / (pl->smem + 1024));  // 228 KB of shared memory per SM
+            pl->grid = std::max(pl->grid, std::min(3, std::max(1, fit)) * cx.num_sms);
+        }
     } else if (pl->tc) {
         // The occupancy query reports one CTA per SM for this kernel, yet three
         // are resident and run faster (80 registers, ~50 KB of shared memory,
@@ -582,6 +594,8 @@ int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, cons
     rc = enqueue_merge(static_cast<Entry *>(cx.lists_a.p), static_cast<Entry *>(cx.lists_b.p), nl, pl.kpad, st,
                        &cur, &launches);
     if (rc) return rc;
+    cx.fin = cur;
+    cx.fin_kpad = pl.kpad;
     CSX_CUDA(mark(4));
     if (full) {
         FullScreenArgs F;
@@ -724,6 +738,215 @@ int csx_screen_full_device(const csx_cfg *cfg, const csx_model_full *model, cons
 
 namespace csx {
 
+// ---- exact tie order (host half; device half in csx_ties.cuh) ----------------
+
+uint32_t host_okey(float x) {
+    x = x + 0.0f;  // -0 ranks with +0
+    if (x != x) return 0u;
+    uint32_t b;
+    std::memcpy(&b, &x, 4);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+// Heap.offer, src/screen.zig:166-192: a K-slot binary min-heap of f32 scores
+// that rejects a score <= its root once full; slot order is the array order.
+void tie_heap_offer(std::vector<TieHit> &h, size_t k, const TieHit &s) {
+    if (h.size() < k) {
+        h.push_back(s);
+        size_t i = h.size() - 1;
+        while (i > 0) {
+            const size_t par = (i - 1) / 2;
+            if (h[par].score <= h[i].score) break;
+            std::swap(h[par], h[i]);
+            i = par;
+        }
+        return;
+    }
+    if (s.score <= h[0].score) return;
+    h[0] = s;
+    size_t i = 0;
+    for (;;) {
+        const size_t l = 2 * i + 1, r = 2 * i + 2;
+        size_t m = i;
+        if (l < k && h[l].score < h[m].score) m = l;
+        if (r < k && h[r].score < h[m].score) m = r;
+        if (m == i) break;
+        std::swap(h[m], h[i]);
+        i = m;
+    }
+}
+
+// The survivors out[0..cnt) of a whole-stream call, reordered as the
+// reference orders them: the stable sort by score of the concatenated
+// per-stream heaps (src/screen.zig:306-319). The screen ranks equal scores
+// by (stream, index); that differs only inside a stream that holds two
+// survivors of one f32 score, or a survivor at the K-th score (where the
+// heap's history decides which tied candidates it kept). Such a stream's
+// heap is replayed exactly: a candidate enters it only if it scores above
+// the root, and the root only grows, so the stream is read in chunks of
+// doubling length, each collecting (on the GPU, reference-order scores) the
+// candidates above the root the previous chunks left, and the host offers
+// them in index order to a heap with the reference's rules. The final list
+// is the top cnt of those heaps and the other streams' survivors by (score
+// descending, stream, heap slot); candidates taken from the replayed heaps
+// are regenerated on the GPU. The precision form (FP64 ranking) has no
+// reference counterpart and keeps (stream, index).
+// The device buffers a finished screen left behind: its elite table, work
+// items (n_items of them), ids and tribes.
+struct ScreenBufs {
+    const float *tab;
+    const Item *items;
+    uint64_t n_items;
+    const unsigned long long *ids;
+    const unsigned int *tribes;
+    const Entry *fin;  // the final top-kpad list (its entry past the survivors shows a tie at the K-th score)
+    uint32_t kpad;
+};
+
+int fix_ties(Context &cx, const csx_cfg &cfg, const csx_model &model, const csx_model_full *full, int ne,
+             uint64_t t_begin, uint64_t t_end, csx_survivor *out, uint64_t cnt, const ScreenBufs &bufs,
+             cudaStream_t st) {
+    const uint64_t n_items = bufs.n_items;
+    if (cnt == 0) return CSX_OK;
+    const uint32_t tau = host_okey(out[cnt - 1].score);
+    // a candidate outside the survivors ties with the K-th score when the
+    // final list's next entry does (the lists keep K + 1 entries, and every
+    // candidate scoring at least the running threshold entered them)
+    bool boundary = false;
+    if (cnt < bufs.kpad && bufs.fin) {
+        Entry next{};
+        CSX_CUDA(cudaMemcpyAsync(&next, bufs.fin + cnt, sizeof(Entry), cudaMemcpyDeviceToHost, st));
+        CSX_CUDA(cudaStreamSynchronize(st));
+        boundary = next.k1 != 0ull && static_cast<uint32_t>(next.k1 >> 32) == tau;
+    }
+    std::set<uint64_t> S;
+    std::map<std::pair<uint64_t, uint32_t>, int> seen;
+    for (uint64_t q = 0; q < cnt; ++q) {
+        const uint32_t ok = host_okey(out[q].score);
+        if (boundary && ok == tau) S.insert(out[q].stream);
+        if (++seen[{out[q].stream, ok}] == 2) S.insert(out[q].stream);
+    }
+    if (S.empty()) return CSX_OK;
+    Plan pl;
+    int rc = make_plan(cx, cfg, model, ne, &pl, 0, 0, 0, t_begin, t_end, full);
+    if (rc) return rc;
+    const StreamGeom &g = pl.g;
+    const SynthConst sc = make_synth(cfg, ne);
+    const ScreenArgs A = screen_args(cfg, model, sc, pl, bufs.tab, bufs.items, nullptr, nullptr);
+    FullScreenArgs F;
+    static_cast<ScreenArgs &>(F) = A;
+    if (full) F.fm = make_full_model(*full);
+    const unsigned int cap = 1u << 20;
+    CSX_CUDA(cx.tie_hits.ensure(static_cast<size_t>(cap) * sizeof(TieHit)));
+    CSX_CUDA(cx.tie_count.ensure(sizeof(unsigned int)));
+    auto *d_hits = static_cast<TieHit *>(cx.tie_hits.p);
+    auto *d_count = static_cast<unsigned int *>(cx.tie_count.p);
+    const int blocks = static_cast<int>(std::min<uint64_t>((n_items + 255) / 256, 32ull * cx.num_sms));
+    const size_t K = static_cast<size_t>(cfg.keep);
+    std::map<uint64_t, std::vector<TieHit>> heaps;
+    std::vector<TieHit> hits;
+    for (uint64_t t : S) {
+        const uint64_t n_t = (t == g.T - 1) ? g.my_last : g.per;
+        std::vector<TieHit> &h = heaps[t];
+        uint64_t lo = 0, size = std::max<uint64_t>(4 * K, 1024);
+        bool all = true;
+        float thr = -INFINITY;
+        while (lo < n_t) {
+            const uint64_t hi = std::min(n_t, lo + size);
+            CSX_CUDA(cudaMemsetAsync(d_count, 0, sizeof(unsigned int), st));
+            const uint32_t ts = static_cast<uint32_t>(t);
+            if (full) {
+                if (pl.fast_delta)
+                    tie_collect_kernel<true><<<blocks, 256, 0, st>>>(F, n_items, ts, lo, hi, thr, all, d_hits, d_count, cap);
+                else
+                    tie_collect_kernel<false><<<blocks, 256, 0, st>>>(F, n_items, ts, lo, hi, thr, all, d_hits, d_count, cap);
+            } else {
+                if (pl.fast_delta)
+                    tie_collect_kernel<true><<<blocks, 256, 0, st>>>(A, n_items, ts, lo, hi, thr, all, d_hits, d_count, cap);
+                else
+                    tie_collect_kernel<false><<<blocks, 256, 0, st>>>(A, n_items, ts, lo, hi, thr, all, d_hits, d_count, cap);
+            }
+            CSX_CUDA(cudaGetLastError());
+            unsigned int n = 0;
+            CSX_CUDA(cudaMemcpyAsync(&n, d_count, sizeof(n), cudaMemcpyDeviceToHost, st));
+            CSX_CUDA(cudaStreamSynchronize(st));
+            if (n > cap) {  // too many above the root in this chunk: read it in halves
+                size = std::max<uint64_t>(1, (hi - lo) / 2);
+                continue;
+            }
+            hits.resize(n);
+            if (n) {
+                CSX_CUDA(cudaMemcpyAsync(hits.data(), d_hits, n * sizeof(TieHit), cudaMemcpyDeviceToHost, st));
+                CSX_CUDA(cudaStreamSynchronize(st));
+            }
+            std::sort(hits.begin(), hits.end(), [](const TieHit &a, const TieHit &b) { return a.index < b.index; });
+            for (const TieHit &x : hits) tie_heap_offer(h, K, x);
+            if (h.size() == K) {
+                all = false;
+                thr = h[0].score;
+            }
+            lo = hi;
+            size *= 2;
+        }
+    }
+    // the reference's order over the replayed heaps and the other survivors
+    struct Ranked {
+        uint32_t okey;
+        uint64_t stream, pos;
+        int64_t from_out;  // survivor index, or -1 - (replayed candidate index)
+    };
+    std::vector<Ranked> all_r;
+    std::vector<TieHit> rep_hits;
+    std::vector<uint64_t> rep_streams;
+    for (uint64_t q = 0; q < cnt; ++q)
+        if (!S.count(out[q].stream))
+            all_r.push_back({host_okey(out[q].score), out[q].stream, out[q].index, static_cast<int64_t>(q)});
+    for (auto &kv : heaps)
+        for (size_t i = 0; i < kv.second.size(); ++i) {
+            const uint32_t ok = host_okey(kv.second[i].score);
+            if (ok < tau) continue;
+            all_r.push_back({ok, kv.first, i, -1 - static_cast<int64_t>(rep_hits.size())});
+            rep_hits.push_back(kv.second[i]);
+            rep_streams.push_back(kv.first);
+        }
+    if (all_r.size() < cnt) return CSX_ERR_DEVICE_STATE;  // cannot happen: the heaps hold every candidate >= tau
+    std::stable_sort(all_r.begin(), all_r.end(), [](const Ranked &a, const Ranked &b) {
+        if (a.okey != b.okey) return a.okey > b.okey;
+        if (a.stream != b.stream) return a.stream < b.stream;
+        return a.pos < b.pos;
+    });
+    const uint32_t nrep = static_cast<uint32_t>(rep_hits.size());
+    std::vector<csx_survivor> regen(nrep);
+    if (nrep) {
+        CSX_CUDA(cx.tie_streams.ensure(nrep * sizeof(uint64_t)));
+        CSX_CUDA(cx.tie_out.ensure(nrep * sizeof(csx_survivor)));
+        CSX_CUDA(cudaMemcpyAsync(d_hits, rep_hits.data(), nrep * sizeof(TieHit), cudaMemcpyHostToDevice, st));
+        CSX_CUDA(cudaMemcpyAsync(cx.tie_streams.p, rep_streams.data(), nrep * sizeof(uint64_t),
+                                 cudaMemcpyHostToDevice, st));
+        auto *d_str = static_cast<const uint64_t *>(cx.tie_streams.p);
+        auto *d_out = static_cast<csx_survivor *>(cx.tie_out.p);
+        const unsigned long long *ids = bufs.ids;
+        const unsigned int *tribes = bufs.tribes;
+        const int rb = unit_blocks(nrep, 128);
+        if (full && pl.fast_delta) tie_regen_full_kernel<true><<<rb, 128, 0, st>>>(F, d_hits, d_str, nrep, ids, tribes, d_out);
+        else if (full) tie_regen_full_kernel<false><<<rb, 128, 0, st>>>(F, d_hits, d_str, nrep, ids, tribes, d_out);
+        else if (pl.fast_delta) tie_regen_kernel<true><<<rb, 128, 0, st>>>(A, d_hits, d_str, nrep, ids, tribes, d_out);
+        else tie_regen_kernel<false><<<rb, 128, 0, st>>>(A, d_hits, d_str, nrep, ids, tribes, d_out);
+        CSX_CUDA(cudaGetLastError());
+        CSX_CUDA(cudaMemcpyAsync(regen.data(), d_out, nrep * sizeof(csx_survivor), cudaMemcpyDeviceToHost, st));
+        CSX_CUDA(cudaStreamSynchronize(st));
+        for (uint32_t i = 0; i < nrep; ++i)  // the regenerated score is the replayed one, bit for bit
+            if (host_okey(regen[i].score) != host_okey(rep_hits[i].score)) return CSX_ERR_DEVICE_STATE;
+    }
+    std::vector<csx_survivor> fixed(cnt);
+    for (uint64_t q = 0; q < cnt; ++q) {
+        const Ranked &r = all_r[q];
+        fixed[q] = r.from_out >= 0 ? out[r.from_out] : regen[static_cast<size_t>(-1 - r.from_out)];
+    }
+    std::copy(fixed.begin(), fixed.end(), out);
+    return CSX_OK;
+}
+
 // csx_screen / csx_screen_range: host buffers, a private stream, synchronous.
 int screen_host(const csx_cfg *cfg, const csx_model *model, const csx_genome *elites, int n_elites,
                 uint64_t t_begin, uint64_t t_end, csx_survivor *out, uint64_t out_cap, uint64_t *n_out,
@@ -764,6 +987,16 @@ int screen_host(const csx_cfg *cfg, const csx_model *model, const csx_genome *el
             if (e == cudaSuccess && res[2] == 0 && cnt > 0 && !(cfg->flags & CSX_FLAG_AS_SHIPPED)) {
                 e = cudaMemcpyAsync(out, ds, cnt * sizeof(csx_survivor), cudaMemcpyDeviceToHost, st);
                 if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+                // whole streams only: an item share does not hold a stream's heap
+                if (e == cudaSuccess && shard.count == 1 &&
+                    !(cfg->flags & (CSX_FLAG_TC_BF16 | CSX_FLAG_TC_FP16)))
+                    rc = fix_ties(*cx, *cfg, *model, full, n_elites, t_begin, t_end, out, cnt,
+                                  ScreenBufs{static_cast<const float *>(cx->tab.p),
+                                             static_cast<const Item *>(cx->items.p), res[3],
+                                             static_cast<const unsigned long long *>(cx->ids.p),
+                                             static_cast<const unsigned int *>(cx->tribes.p), cx->fin,
+                                             cx->fin_kpad},
+                                  st);
             }
         }
     }

@@ -165,19 +165,20 @@ __global__ void __launch_bounds__(kThreads, 3) screen_kernel(const __grid_consta
         for (int r = 0; r < kRounds && valid && !has_def; ++r) {
             const CandHead h = cand_head(A.sc, seed_t, p);
             const float s = cand_score<kFastDelta>(A, el, seed_t, p, h);
+            // every candidate scoring at least the threshold enters the buffer,
+            // ties with the running K-th score included: the final list's
+            // (K+1)-th entry is then exact (exact-tie detection)
             if (s >= ts) {
                 const unsigned long long k1 =
                     (static_cast<unsigned long long>(score_okey(s)) << 32) | static_cast<unsigned int>(~item);
                 const unsigned long long k2 =
                     (static_cast<unsigned long long>(~dcand) << 32) | ddraw;
-                if (k1 > t1 || (k1 == t1 && k2 > t2)) {
-                    const unsigned int slot = atomicAdd(&s_buf_n, 1u);
-                    if (slot < A.buf_cap) {
-                        buf[slot] = Entry{k1, k2};
-                    } else {
-                        has_def = true;
-                        def = Entry{k1, k2};
-                    }
+                const unsigned int slot = atomicAdd(&s_buf_n, 1u);
+                if (slot < A.buf_cap) {
+                    buf[slot] = Entry{k1, k2};
+                } else {
+                    has_def = true;
+                    def = Entry{k1, k2};
                 }
             }
             p += h.len;
@@ -265,7 +266,7 @@ __global__ void __launch_bounds__(kThreads, 2) screen_q_kernel(const __grid_cons
             const unsigned long long k1 =
                 (static_cast<unsigned long long>(score_okey(s)) << 32) | static_cast<unsigned int>(~q.item);
             const unsigned long long k2 = (static_cast<unsigned long long>(~q.dcand) << 32) | q.ddraw;
-            if (k1 > t1 || (k1 == t1 && k2 > t2)) buf[atomicAdd(&s_buf_n, 1u)] = Entry{k1, k2};
+            buf[atomicAdd(&s_buf_n, 1u)] = Entry{k1, k2};  // score >= ts: ties with the K-th kept
         }
     };
 
@@ -529,6 +530,7 @@ __global__ void __launch_bounds__(kThreads, 3) screen_tc_kernel(const __grid_con
     Pend *pend = reinterpret_cast<Pend *>(el + (A.sc.ne + 1) * kNtot);
     __shared__ __align__(8) unsigned long long s_mbar[2];
     __shared__ uint32_t s_tbase;
+    __shared__ uint32_t s_gbad[2], s_fail_phase[2];
     __shared__ unsigned int s_buf_n, s_pend_n;
     __shared__ unsigned long long s_t1, s_t2;
     __shared__ float s_ts;
@@ -546,6 +548,8 @@ __global__ void __launch_bounds__(kThreads, 3) screen_tc_kernel(const __grid_con
     if (tid == 0) {
         mbar_init(smem_u32(&s_mbar[0]), 1);
         mbar_init(smem_u32(&s_mbar[1]), 1);
+        s_gbad[0] = s_gbad[1] = 0;
+        s_fail_phase[0] = s_fail_phase[1] = 0;
         s_buf_n = 0;
         s_pend_n = 0;
         s_t1 = 0;
@@ -597,7 +601,7 @@ __global__ void __launch_bounds__(kThreads, 3) screen_tc_kernel(const __grid_con
             const unsigned long long k1 =
                 (static_cast<unsigned long long>(score_okey(sf)) << 32) | static_cast<unsigned int>(~q.item);
             const unsigned long long k2 = (static_cast<unsigned long long>(~q.dcand) << 32) | q.ddraw;
-            if (k1 > t1 || (k1 == t1 && k2 > t2)) buf[atomicAdd(&s_buf_n, 1u)] = Entry{k1, k2};
+            buf[atomicAdd(&s_buf_n, 1u)] = Entry{k1, k2};  // score >= ts: ties with the K-th kept
         }
     };
 
@@ -622,7 +626,9 @@ __global__ void __launch_bounds__(kThreads, 3) screen_tc_kernel(const __grid_con
     for (;;) {
         __syncthreads();
         const unsigned int pn = min(s_pend_n, kPendCap);
-        const int any = __syncthreads_or(valid || has_def);
+        // a group whose tensor-core wait gave up ends the CTA's screening
+        const int stop = (s_gbad[0] | s_gbad[1]) != 0u;
+        const int any = __syncthreads_or((valid || has_def) && !stop);
         const int any_def = __syncthreads_or(has_def);
         // the queue is scored once it can employ every thread (or a thread
         // waits on it, or the work is done); a flush appends <= pn + 256 <= 768
@@ -675,7 +681,7 @@ __global__ void __launch_bounds__(kThreads, 3) screen_tc_kernel(const __grid_con
                 for (int i = 0; i < 16; ++i) x[i] = 0.0f;
             }
             float y[16];
-            tc_ok = tc_round(tg, pk, tid & 127u, y) && tc_ok;
+            if (!tcp_round(tg, pk, tid & 127u, y, &s_gbad[grp], &s_fail_phase[grp])) tc_ok = false;
             if (act) {
                 float s = R;
 #pragma unroll
@@ -720,6 +726,8 @@ __global__ void __launch_bounds__(kThreads, 3) screen_tc_kernel(const __grid_con
         atomicAdd(&A.ctrl->exact_evals, exact);
     }
     if (!tc_ok) atomicOr(&A.ctrl->err, kErrTc);
+    __syncthreads();
+    if (s_gbad[grp] != 0u && tg.issuer) (void)mbar_wait(tg.mbar, s_fail_phase[grp]);  // bounded
     tc_fence_before();
     __syncthreads();
     tc_fence_after();

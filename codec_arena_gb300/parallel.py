@@ -50,15 +50,23 @@ def item_shard(rank: int, world: int):
 
 
 def merge_survivors(parts: Iterable[np.ndarray], keep: int) -> np.ndarray:
-    """Global top-`keep` of per-rank survivor lists, in the reference's final
-    order: score descending, ties by (stream, index) ascending."""
-    parts = [np.asarray(p, dtype=SURVIVOR_DTYPE) for p in parts if len(p)]
-    if not parts:
+    """Global top-`keep` of per-rank survivor lists (in rank order), in the
+    reference's final order: score descending, then stream, then each list's
+    own order. A stream lives in one rank's list when the generation is split
+    by stream (that list already orders its exact ties as the reference's
+    heap does), and in consecutive ranks' lists in index order when it is
+    split by work items, so (rank, position) continues the order either way."""
+    parts = [np.asarray(p, dtype=SURVIVOR_DTYPE) for p in parts]
+    keys = [(np.full(len(p), r), np.arange(len(p))) for r, p in enumerate(parts)]
+    if not any(len(p) for p in parts):
         return np.zeros(0, dtype=SURVIVOR_DTYPE)
     a = np.concatenate(parts)
+    rank = np.concatenate([k[0] for k in keys])
+    pos = np.concatenate([k[1] for k in keys])
     # NaN scores never survive (they have no order in the reference)
-    a = a[~np.isnan(a["score"])]
-    order = np.lexsort((a["index"], a["stream"], -a["score"].astype(np.float64)))
+    ok = ~np.isnan(a["score"])
+    a, rank, pos = a[ok], rank[ok], pos[ok]
+    order = np.lexsort((pos, rank, a["stream"], -a["score"].astype(np.float64)))
     return a[order][: int(keep)]
 
 

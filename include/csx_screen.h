@@ -146,7 +146,10 @@ int csx_survivor_format_line(const csx_survivor *s, uint32_t flags, char *buf, s
 
 /* run(), src/screen.zig:257-343, without the file output: host buffers in and
  * out. Writes min(keep, lambda) survivors (0 with CSX_FLAG_AS_SHIPPED) sorted
- * by score descending, ties by (stream, index) ascending; *screened is the
+ * by score descending, then stream ascending, and exact f32 ties inside a
+ * stream as the reference's per-stream heap ranks them (src/screen.zig:
+ * 151-193,306-319; those streams' heaps are replayed exactly: the rare calls
+ * that hold such ties take longer); *screened is the
  * candidate count the reference writes to --count-out. Synchronous. */
 int csx_screen(const csx_cfg *cfg, const csx_model *model, const csx_genome *elites,
                int n_elites, csx_survivor *out, uint64_t out_cap, uint64_t *n_out,
@@ -179,6 +182,8 @@ int csx_screen_items(const csx_cfg *cfg, const csx_model *model, const csx_genom
                      uint64_t *screened);
 
 /* Same, with device-resident elites and survivors, enqueued on `cuda_stream`
+ * (exact f32 ties inside one stream ranked by index: the heap replay needs
+ * the host; so do csx_screen_items shares and csx_screen_batch_device)
  * (a cudaStream_t; NULL = the legacy default stream). d_result receives four
  * device uint64: survivor count, screened count, device error bits (0 = ok)
  * and the number of work items screened. The call returns after enqueueing; calls on different

@@ -99,14 +99,13 @@ def test_full_model_wrong_size(csx, n):
 
 def _check_screen(orc, lam, keep, seed, T, w, el, **kw):
     from codec_arena_gb300 import screen
-    from test_gpu_screen import assert_same_modulo_ties
 
     cfg = screen.Cfg(lam, keep, seed, threads=T, **kw)
     got, sg = screen.screen(cfg, screen.ModelFull.from_compact(w), el)
     oc = orc.cfg(lam, keep, seed, threads=T, **kw)
     want, sw = orc.screen(oc, orc.model_full_from_compact(w), el, cpu_threads=8)
     assert sg == sw
-    assert_same_modulo_ties(got, want)
+    assert got.tobytes() == want.tobytes()
     return got
 
 

@@ -6,7 +6,6 @@ import os
 
 import numpy as np
 import pytest
-from test_gpu_screen import assert_same_modulo_ties
 
 pytestmark = pytest.mark.gpu
 
@@ -48,9 +47,9 @@ def test_random_config_matches_oracle(orc, i):
     oc = orc.cfg(lam, keep, seed, threads=T, sigma=sigma, jump_p=jump, imm_p=imm)
     want, wn = orc.screen(oc, orc.model_from_compact(w), el, cpu_threads=os.cpu_count() or 4)
     assert n == wn == lam
-    # pure crossover (sigma 0, no jumps or immigrants) makes exact f32 ties common:
-    # the same score sequence, and the same candidates at every score above the boundary
-    assert_same_modulo_ties(got, want)
+    # pure crossover (sigma 0, no jumps or immigrants) makes exact f32 ties common;
+    # the screen replays the heaps of the streams that hold them
+    assert got.tobytes() == want.tobytes()
 
 
 @pytest.mark.parametrize("b", range(6))
@@ -89,4 +88,4 @@ def test_random_config_full_surface_matches_oracle(orc, i):
     oc = orc.cfg(lam, keep, seed, threads=T, sigma=sigma, jump_p=jump, imm_p=imm)
     want, wn = orc.screen(oc, orc.model_full_from_compact(w), el, cpu_threads=os.cpu_count() or 4)
     assert n == wn == lam
-    assert_same_modulo_ties(got, want)
+    assert got.tobytes() == want.tobytes()
