@@ -88,6 +88,9 @@ def parse(argv=None):
                     help="islands: 20 islands batched in one graph launch (not the headline line); "
                          "config1: the reference workload's first configuration (lambda 1e6, top 32, "
                          "seeded 153-term surface)")
+    ap.add_argument("--split", default="islands", choices=["islands", "items"],
+                    help="N > 1 GPUs: one island per rank (weak scaling), or one generation split by work "
+                         "items across the ranks with a survivor gather (strong scaling)")
     ap.add_argument("--islands", type=int, default=20)
     ap.add_argument("--islands-scale", type=float, default=1.0,
                     help="scale every island budget (small cases for profiling)")
@@ -749,10 +752,71 @@ def run_config1(args):
     print(json.dumps(line), flush=True)
 
 
+def run_split_items(args):
+    """`--split items` on N GPUs: ONE generation (the default workload) split
+    across the ranks by work items (csx_screen_items), the ranks' survivors
+    gathered and merged (parallel.gather_survivors): strong scaling. Each step
+    is the host-buffer call plus the gather, timed on the host around a
+    barrier, the max over ranks."""
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from codec_arena_gb300 import parallel, screen, workloads as wl
+
+    el = wl.seeded_elites(N_ELITES)
+    model = screen.Model.from_compact(wl.surrogate_161())
+    cfg = screen.Cfg(args.lam, args.keep, SEED, threads=args.threads)
+
+    def step():
+        mine, n = screen.screen(cfg, model, el, items=parallel.item_shard(rank, world))
+        return parallel.gather_survivors(mine, args.keep, device="cuda"), n
+
+    for _ in range(max(3, args.warmup)):
+        merged, _ = step()
+    sampler = ClockSampler(local)
+    sampler.start()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    scr = 0
+    for _ in range(args.steps):
+        merged, n = step()
+        scr += n
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    dt = parallel.max_over_ranks(time.perf_counter() - t0, device="cuda")
+    clocks = sampler.stop()
+    total = parallel.max_over_ranks(float(scr), device="cuda")  # per rank: its share's count
+    if rank != 0:
+        return
+    value = args.lam * args.steps / dt
+    line = {"metric": METRIC, "value": value, "unit": "candidates/s", "n_gpus": world, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": 1000 * dt / args.steps, "higher_is_better": True,
+            "scaling": "strong", "vs_baseline": value / PUBLISHED_CAND_S, "vs_baseline_source": PUBLISHED_SOURCE,
+            "dtype": "u64/f32", "data": "synthetic (seeded)",
+            "config": dict(workload_config(args, 1), parallelism=f"items{world}",
+                           split="one generation split by work items across the ranks, survivors gathered"),
+            "e2e": {"value": value, "unit": "candidates/s", "h2d_bytes_per_step": int(el.nbytes),
+                    "d2h_bytes_per_step": int(args.keep * 168),
+                    "api": "csx_screen_items (host buffers) + gather_survivors, every step"},
+            "best_score": float(merged["score"][0]) if len(merged) else None,
+            "largest_share_screened": total / args.steps, "clocks": clocks}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.workload == "config1" and args.impl != "reference":
         return run_config1(args)
+    if args.split == "items" and args.impl != "reference" and args.workload == "generation":
+        return run_split_items(args)
     if args.workload == "refit" and args.impl != "reference":
         return run_refit(args)
     if args.workload == "full" and args.impl != "reference":
