@@ -394,6 +394,10 @@ struct BatchLayout {
     Ctrl *ctrl_all = nullptr;
     Entry *lists_all = nullptr;
     size_t lists_bytes = 0;
+    // the pruned batch: every island's pruning screen (csx_prune.cuh) in turn
+    bool prune = false;
+    std::vector<PruneArgs> pargs;
+    uint32_t *pub = nullptr;  // kPruneMs x grid, cleared before each island
 };
 
 int batch_context_init(Context &cx) {
@@ -425,35 +429,63 @@ int batch_prepare(Context &cx, int n, const csx_cfg *cfgs, const csx_model *mode
                           (c.sigma == 0.0f || std::fabs(c.sigma) >= 1.0e-30f);
         L->fast = L->fast && fast;
         L->filter = L->filter && !(c.flags & CSX_FLAG_EXACT_ALL) && filter_bound(models[i]) > 0.0f;
-        const uint32_t kpad = std::max<uint32_t>(32, pow2_at_least(c.keep));
+        const uint32_t kpad = list_kpad(c.keep);
         L->kpad_max = std::max(L->kpad_max, kpad);
         L->keep_max = std::max<uint32_t>(L->keep_max, static_cast<uint32_t>(c.keep));
         L->sort_n = std::max(L->sort_n, pow2_at_least(kpad + 4ull * kThreads));
         ne_max = std::max(ne_max, n_elites[i]);
     }
     L->ne_max = static_cast<uint32_t>(ne_max);
-    L->smem = screen_smem(L->sort_n, ne_max, L->filter);
-    if (L->smem + 2048 > cx.max_smem) return CSX_ERR_LIMIT;
-    BatchFn fn = batch_fn(L->fast, L->filter);
-    CSX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(L->smem)));
-    int per_sm = 0;
-    CSX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, L->smem));
-    per_sm = std::max(1, per_sm);
-    if (tune && tune->ctas_per_sm > 0) per_sm = std::min<int>(per_sm, static_cast<int>(tune->ctas_per_sm));
-    L->grid = per_sm * cx.num_sms;
-    const size_t msmem = 2ull * L->kpad_max * sizeof(Entry);
-    CSX_CUDA(cudaFuncSetAttribute(merge_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  static_cast<int>(msmem)));
 
+    // plans (the grid is set below; item and segment sizes do not depend on it)
     uint64_t items_sum = 0;
+    L->prune = true;
     for (int i = 0; i < n; ++i) {
         if (cfgs[i].lambda == 0) continue;
-        int rc = make_plan(cx, cfgs[i], models[i], n_elites[i], &L->pl[i], L->grid, tune ? tune->item_cands : 0,
+        int rc = make_plan(cx, cfgs[i], models[i], n_elites[i], &L->pl[i], 1, tune ? tune->item_cands : 0,
                            tune ? tune->seg_cands : 0);
         if (rc) return rc;
         items_sum += L->pl[i].items_cap;
+        L->prune = L->prune && L->pl[i].prune_ok && L->pl[i].prune_tc;
     }
     if (items_sum >= 0xFFFFFFFFull) return CSX_ERR_LIMIT;
+
+    int per_sm = 0;
+    const int cap = tune && tune->ctas_per_sm > 0 ? static_cast<int>(tune->ctas_per_sm) : 3;
+    if (L->prune) {
+        // every island's pruning screen with the tensor-core bound, one after
+        // another, each with its own shared memory and up to three CTAs per SM
+        // (as the single screen); the lists are laid out for the widest grid
+        L->smem = 0;
+        for (int i = 0; i < n; ++i) {
+            if (cfgs[i].lambda == 0) continue;
+            Plan &pl = L->pl[i];
+            pl.smem = prune_smem(pl.sort_n, n_elites[i], pl.nb, cx.num_sms, true);
+            if (pl.smem + 1024 > cx.max_smem) return CSX_ERR_LIMIT;
+            const int fit = std::min(cap, std::max(1, static_cast<int>((228u << 10) / (pl.smem + 1024))));
+            pl.grid = fit * cx.num_sms;
+            L->smem = std::max(L->smem, pl.smem);
+            per_sm = std::max(per_sm, fit);
+        }
+        per_sm = std::max(per_sm, 1);
+        for (int nb : {16, kNtot})
+            CSX_CUDA(cudaFuncSetAttribute(screen_p_fn(nb, true, true, false),
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(L->smem)));
+    } else {
+        L->smem = screen_smem(L->sort_n, ne_max, L->filter);
+        if (L->smem + 2048 > cx.max_smem) return CSX_ERR_LIMIT;
+        BatchFn fn = batch_fn(L->fast, L->filter);
+        CSX_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(L->smem)));
+        CSX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, L->smem));
+        per_sm = std::max(1, per_sm);
+    }
+    if (tune && tune->ctas_per_sm > 0) per_sm = std::min(per_sm, cap);
+    L->grid = per_sm * cx.num_sms;
+    if (!L->prune)
+        for (int i = 0; i < n; ++i) L->pl[i].grid = L->grid;
+    const size_t msmem = 2ull * L->kpad_max * sizeof(Entry);
+    CSX_CUDA(cudaFuncSetAttribute(merge_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(msmem)));
 
     // carve: a sizing pass, then the real one
     const uint32_t nl = static_cast<uint32_t>(L->grid);
@@ -463,9 +495,10 @@ int batch_prepare(Context &cx, int n, const csx_cfg *cfgs, const csx_model *mode
         L->d_base = cv.take<unsigned int>(n + 1);
         L->d_next = cv.take<unsigned int>(1);
         L->ctrl_all = cv.take<Ctrl>(n);
+        L->pub = L->prune ? cv.take<uint32_t>(static_cast<size_t>(kPruneMs) * nl) : nullptr;
         const size_t lists0 = (cv.off + 255) & ~static_cast<size_t>(255);
         for (int i = 0; i < n; ++i) {
-            const uint32_t kpad = std::max<uint32_t>(32, pow2_at_least(cfgs[i].keep));
+            const uint32_t kpad = list_kpad(cfgs[i].keep);
             L->b[i].la = cv.take<Entry>(static_cast<size_t>(nl) * kpad);
         }
         L->lists_all = reinterpret_cast<Entry *>(base + lists0);
@@ -473,7 +506,7 @@ int batch_prepare(Context &cx, int n, const csx_cfg *cfgs, const csx_model *mode
         for (int i = 0; i < n; ++i) {
             IslandBufs &b = L->b[i];
             const Plan &pl = L->pl[i];
-            const uint32_t kpad = std::max<uint32_t>(32, pow2_at_least(cfgs[i].keep));
+            const uint32_t kpad = list_kpad(cfgs[i].keep);
             b.ctrl = L->ctrl_all + i;
             b.lb = cv.take<Entry>(static_cast<size_t>((nl + 1) / 2) * kpad);
             b.tab = cv.take<float>(static_cast<size_t>(n_elites[i] + 1) * kNtot);
@@ -521,11 +554,26 @@ int batch_prepare(Context &cx, int n, const csx_cfg *cfgs, const csx_model *mode
         d.out = d_out + out_off;
         d.result = d_result + 4 * i;
         d.keep = static_cast<uint32_t>(cfgs[i].keep);
-        d.kpad = std::max<uint32_t>(32, pow2_at_least(cfgs[i].keep));
+        d.kpad = list_kpad(cfgs[i].keep);
         d.ne = static_cast<uint32_t>(n_elites[i]);
         d.err = filter_bound(models[i]);
         jump_bound(models[i], &d.jb);
         out_off += cfgs[i].keep;
+    }
+    L->pargs.assign(n, PruneArgs{});
+    if (L->prune) {
+        for (int i = 0; i < n; ++i) {
+            if (cfgs[i].lambda == 0) continue;
+            const Plan &pl = L->pl[i];
+            const IslandBufs &b = L->b[i];
+            PruneArgs &P = L->pargs[i];
+            static_cast<ScreenArgs &>(P) = screen_args(cfgs[i], models[i], make_synth(cfgs[i], n_elites[i]), pl,
+                                                       b.tab, b.items, b.ctrl, b.la);
+            P.pc = pl.pc;
+            P.tc = pl.ptc;
+            P.pub = L->pub;
+            P.sel_cap = 8u * static_cast<uint32_t>(cx.num_sms);
+        }
     }
     return CSX_OK;
 }
@@ -560,20 +608,34 @@ int batch_enqueue(Context &cx, const BatchLayout &L, cudaStream_t st, bool captu
             if (rc) return rc;
         }
         CSX_CUDA(cudaEventRecord(cx.ev_join[i], a));
-        CSX_CUDA(cudaStreamWaitEvent(st, cx.ev_join[i], 0));
+        if (!L.prune) CSX_CUDA(cudaStreamWaitEvent(st, cx.ev_join[i], 0));
     }
-    batch_base_kernel<<<1, 32, 0, st>>>(L.d_isl, static_cast<uint32_t>(n), L.d_base, L.d_next);
-    CSX_CUDA(cudaGetLastError());
-    BatchArgs B;
-    B.isl = L.d_isl;
-    B.base = L.d_base;
-    B.next_item = L.d_next;
-    B.n_islands = static_cast<uint32_t>(n);
-    B.sort_n = L.sort_n;
-    B.ne_max = L.ne_max;
-    batch_fn(L.fast, L.filter)<<<L.grid, kThreads, L.smem, st>>>(B);
-    CSX_CUDA(cudaGetLastError());
-    nk += 2;
+    if (L.prune) {
+        // island i's screen waits only for island i's items: the later
+        // islands' item building overlaps the earlier screens
+        for (int i = 0; i < n; ++i) {
+            CSX_CUDA(cudaStreamWaitEvent(st, cx.ev_join[i], 0));
+            if (L.cfg[i].lambda == 0) continue;
+            const Plan &pl = L.pl[i];
+            CSX_CUDA(cudaMemsetAsync(L.pub, 0, static_cast<size_t>(kPruneMs) * pl.grid * sizeof(uint32_t), st));
+            screen_p_fn(pl.nb, true, true, false)<<<pl.grid, kThreads, pl.smem, st>>>(L.pargs[i]);
+            CSX_CUDA(cudaGetLastError());
+            ++nk;
+        }
+    } else {
+        batch_base_kernel<<<1, 32, 0, st>>>(L.d_isl, static_cast<uint32_t>(n), L.d_base, L.d_next);
+        CSX_CUDA(cudaGetLastError());
+        BatchArgs B;
+        B.isl = L.d_isl;
+        B.base = L.d_base;
+        B.next_item = L.d_next;
+        B.n_islands = static_cast<uint32_t>(n);
+        B.sort_n = L.sort_n;
+        B.ne_max = L.ne_max;
+        batch_fn(L.fast, L.filter)<<<L.grid, kThreads, L.smem, st>>>(B);
+        CSX_CUDA(cudaGetLastError());
+        nk += 2;
+    }
     const size_t msmem = 2ull * L.kpad_max * sizeof(Entry);
     uint32_t nl = static_cast<uint32_t>(L.grid);
     int in_b = 0;

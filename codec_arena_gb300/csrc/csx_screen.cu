@@ -146,6 +146,7 @@ struct Plan {
     float err = 0.0f;
     JumpBound jb{};  // widening of err for a candidate with a jump (filter mode)
     bool prune = false;     // the pruning screen (csx_prune.cuh)
+    bool prune_ok = false;  // its bound is certifiable for this call (the batch decides for itself)
     bool prune_tc = false;  // its bound's gradient on the tensor cores
     int nb = 16;            // crossover genes its bound draws
     PruneConst pc{};
@@ -265,6 +266,12 @@ int split_streams(const csx_cfg &cfg, uint64_t t_begin, uint64_t t_end, StreamGe
     return CSX_OK;
 }
 
+// Entries of a CTA list: the next power of two above K, so K + 1 entries for K
+// <= 2048 (the final (K+1)-th entry shows a tie at the K-th score: fix_ties).
+uint32_t list_kpad(uint64_t keep) {
+    return std::max<uint32_t>(32, pow2_at_least(keep + (keep <= 2048 ? 1 : 0)));
+}
+
 // Mutation form, filter bounds and the CTA list / buffer sizes of a plan.
 void screen_shape(const csx_cfg &cfg, const csx_model &model, bool full, Plan *pl) {
     pl->fast_delta = std::isfinite(cfg.sigma) && std::fabs(cfg.sigma) <= 1.0e38f &&
@@ -284,10 +291,7 @@ void screen_shape(const csx_cfg &cfg, const csx_model &model, bool full, Plan *p
     pl->prune_tc = pl->prune && (tcf != 0 || !(cfg.flags & CSX_FLAG_PRUNE_FFMA)) &&
                    make_prune_tc(model, pl->pc, tcf != CSX_FLAG_TC_BF16, &pl->ptc);
     if (tcf && !pl->prune_tc) pl->prune = false;
-    // the lists keep K + 1 entries where that fits (keep <= 2048): the final
-    // (K+1)-th entry tells whether a candidate outside the survivors ties with
-    // the K-th score (exact-tie order, fix_ties)
-    pl->kpad = std::max<uint32_t>(32, pow2_at_least(cfg.keep + (cfg.keep <= 2048 ? 1 : 0)));
+    pl->kpad = list_kpad(cfg.keep);
     pl->sort_n = pow2_at_least(pl->kpad + 4ull * kThreads);
     pl->buf_cap = pl->sort_n - pl->kpad;
 }
@@ -295,6 +299,15 @@ void screen_shape(const csx_cfg &cfg, const csx_model &model, bool full, Plan *p
 // Walk segments of about `seg` candidates (g.d_log2 set): L draws rounded to
 // the candidate length when it is constant, the segment counts, and a
 // checkpoint capacity for ck_mult * L / 33 starts.
+// Candidates past its own end that a segment's truth range reaches before its
+// chain meets the next segment's (the link's walk): median ~130, 99th
+// percentile ~12000, largest seen ~15000 over random boundaries of the
+// reference's length rule (62 / 64 / 33 / 35 draws with immigrant 1%, jump
+// 2%). The pooled plan's checkpoints cover at least the segment plus this
+// margin, so short segments keep their items at D candidates; past the last
+// checkpoint a segment's final item grows instead (correct, but serial).
+constexpr uint64_t kLinkSlackCands = 24576;
+
 void segment_geometry(const csx_cfg &cfg, uint64_t seg, uint64_t ck_mult, StreamGeom &g) {
     const uint64_t my_max = std::max(g.per, g.my_last);
     const bool has_last = g.t0 + g.nT == g.T;
@@ -309,7 +322,9 @@ void segment_geometry(const csx_cfg &cfg, uint64_t seg, uint64_t ck_mult, Stream
     g.C = static_cast<uint32_t>(std::max<uint64_t>(1, (64 * g.per + L - 1) / L));
     g.C_last = static_cast<uint32_t>(std::max<uint64_t>(1, (64 * g.my_last + L - 1) / L));
     g.n_seg = (g.nT - 1) * g.C + (has_last ? g.C_last : g.C);
-    g.ckcap = static_cast<uint32_t>((ck_mult * L / 33) / (1ull << g.d_log2) + 3);
+    uint64_t cover = ck_mult * L / 33;  // starts if every candidate were 33 draws long
+    if (ck_mult > 1) cover = std::max<uint64_t>(cover, std::min(seg, my_max) + kLinkSlackCands);
+    g.ckcap = static_cast<uint32_t>(cover / (1ull << g.d_log2) + 3);
 }
 
 // A share of one generation's work items (csx_screen_items): every share
@@ -339,6 +354,7 @@ int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int
     if (full && tcf) return CSX_ERR_BAD_ARGS;  // the precision form scores the reference surface
     pl->tc = tcf != 0;  // FP64 ranking (pruned, or the unpruned precision kernel)
     pl->fp16 = tcf == CSX_FLAG_TC_FP16;
+    pl->prune_ok = pl->prune;
     if (pl->prune && grid_override == 0) {
         // the selection scratch holds one key per CTA: at most 8 CTAs of 256 threads per SM
         pl->smem = prune_smem(pl->sort_n, ne, pl->nb, cx.num_sms, pl->prune_tc);
@@ -397,7 +413,17 @@ int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int
     while ((2ull << dl) <= d) ++dl;  // D = 2^dl <= d
     g.d_log2 = dl;
     const uint64_t D = 1ull << dl;
-    segment_geometry(cfg, seg_cands ? seg_cands : env_u64("CSX_SEG_CANDS", kDefaultSegCands), 2, g);
+    // walk segments: kDefaultSegCands at large budgets; smaller budgets keep
+    // about 256 segments per SM down to 1024 candidates each, since the walk
+    // is serial within a segment (measured at lambda 1e6, T = 4: items 5.1 ms
+    // at 49152, 1.14 at 8192, 0.70 at 1024). Sharded calls size it by the
+    // fixed SM count, like the items.
+    uint64_t seg = seg_cands ? seg_cands : env_u64("CSX_SEG_CANDS", 0);
+    if (seg == 0) {
+        const uint64_t sms = sharded ? kItemRefSms : static_cast<uint64_t>(cx.num_sms);
+        seg = std::min<uint64_t>(kDefaultSegCands, std::max<uint64_t>(1024, lam_range / (256 * sms)));
+    }
+    segment_geometry(cfg, seg, 2, g);
     pl->short_path = my_max <= D;
     pl->items_cap = pl->short_path ? g.nT : g.n_seg * (static_cast<uint64_t>(g.ckcap) + 1);
     if (pl->items_cap >= 0xFFFFFFFFull) return CSX_ERR_LIMIT;

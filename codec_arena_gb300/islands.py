@@ -3,9 +3,12 @@
 An island is what one CI shard of the reference runs each generation
 (brain/evolve.py with its own seed, elites and surrogate;
 .github/workflows/arena.yml:56-92). `screen_batch` screens all islands in one
-CUDA-graph launch of one pipeline (one persistent screen kernel for every
-island's candidates) and returns, per island, exactly what `screen.screen`
-returns for that island alone. `Tune` holds the pipeline's tunables, which
+CUDA-graph launch of one pipeline and returns, per island, exactly what
+`screen.screen` returns for that island alone. The islands' item building runs
+on parallel streams; then, when every island's surrogate admits the pruning
+bound, each island's pruning screen runs in turn over the whole GPU, else one
+unpruned persistent screen kernel takes every island's candidates (a
+FLAG_NO_PRUNE island selects that form for its batch). `Tune` holds the pipeline's tunables, which
 change speed only; `autotune` picks them by timing.
 """
 from __future__ import annotations

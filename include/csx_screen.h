@@ -246,10 +246,14 @@ int csx_last_run_info(csx_run_info *out);
  * Several independent screens ("islands": the reference's CI shards, each
  * running brain/evolve.py with its own seed, elites and surrogate,
  * .github/workflows/arena.yml:56-92) in one pipeline: every island's work
- * items are built on its own forked stream, then ONE persistent screen launch
- * consumes all islands' items and keeps a top-K per island, then one merge
- * tree and one regeneration launch serve all islands. Results per island
- * equal csx_screen's for that island's cfg, model and elites.
+ * items are built on its own forked stream; then, when every island's
+ * surrogate admits the tensor-core pruning bound, each island's pruning
+ * screen runs over the whole GPU in turn, else (or when any island carries
+ * CSX_FLAG_NO_PRUNE) ONE unpruned persistent screen launch consumes all
+ * islands' items and keeps a top-K per island; one merge tree and one
+ * regeneration launch serve all islands. Results per island equal
+ * csx_screen's for that island's cfg, model and elites, exact f32 ties
+ * included (csx_screen_batch; see csx_screen_device for the device call).
  *
  * Tunables do not change results, only speed (0 = automatic). */
 #define CSX_MAX_ISLANDS 64

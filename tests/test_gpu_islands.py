@@ -84,6 +84,25 @@ def test_tunables_do_not_change_results(tune):
         _same(a, b)
 
 
+def test_pruned_and_unpruned_batch_forms_agree():
+    """A batch whose islands all take the tensor-core pruning bound runs one
+    pruning screen per island; one island flagged NO_PRUNE sends the whole
+    batch through the single unpruned batch kernel. Both equal the single
+    screens."""
+    import dataclasses
+
+    from codec_arena_gb300 import _lib, islands
+
+    cfgs, models, elites = _batch(7, 21, 2e4, 3e6, keeps=(16, 256, 1000))
+    pruned = islands.screen_batch(cfgs, models, elites)
+    _check_against_single(cfgs, models, elites, pruned)
+    mixed = [dataclasses.replace(c, flags=_lib.FLAG_NO_PRUNE) if j == 3 else c for j, c in enumerate(cfgs)]
+    unpruned = islands.screen_batch(mixed, models, elites)
+    for (a, na), (b, nb) in zip(pruned, unpruned):
+        assert na == nb
+        _same(a, b)
+
+
 def test_edge_islands():
     """Empty budget, budget below keep, two elites, keep 4096, one stream."""
     from codec_arena_gb300 import screen, islands, workloads as wl
