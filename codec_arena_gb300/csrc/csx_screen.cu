@@ -281,7 +281,6 @@ void screen_shape(const csx_cfg &cfg, const csx_model &model, bool full, Plan *p
     pl->filter = !full && !(cfg.flags & CSX_FLAG_EXACT_ALL) && pl->err > 0.0f;
     // the pruning screen: the filter form's conditions, the fast delta form
     // (its mutation is within |sigma| of the parent gene by construction) and
-    // a certifiable bound; the precision form keeps its own kernel
     // a certifiable bound. The precision form (TC flags) prunes with its tile
     // format's bound and ranks in FP64; without a tensor-core bound it keeps
     // its own unpruned kernel.
