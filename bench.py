@@ -92,6 +92,7 @@ def parse(argv=None):
                     help="N > 1 GPUs: one island per rank (weak scaling), or one generation split by work "
                          "items across the ranks with a survivor gather (strong scaling)")
     ap.add_argument("--islands", type=int, default=20)
+    ap.add_argument("--no-autotune", action="store_true", help="islands: the automatic tunables, no tuning runs")
     ap.add_argument("--islands-scale", type=float, default=1.0,
                     help="scale every island budget (small cases for profiling)")
     return ap.parse_args(argv)
@@ -282,7 +283,10 @@ def run_islands(args):
     t0 = time.perf_counter()
     # tuned on the batch itself (full budgets) over the plausible settings
     cands = [islands.Tune(), islands.Tune(ctas_per_sm=2), islands.Tune(seg_cands=131072)]
-    best, table = autotune.autotune(cfgs, models, elites, candidates=cands, scale=1.0, reps=1)
+    if args.no_autotune:
+        best, table = islands.Tune(), []
+    else:
+        best, table = autotune.autotune(cfgs, models, elites, candidates=cands, scale=1.0, reps=1)
     tune_s = time.perf_counter() - t0
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     for _ in range(max(3, args.warmup)):

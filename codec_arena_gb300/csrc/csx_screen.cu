@@ -297,7 +297,8 @@ void screen_shape(const csx_cfg &cfg, const csx_model &model, bool full, Plan *p
 
 // Walk segments of about `seg` candidates (g.d_log2 set): L draws rounded to
 // the candidate length when it is constant, the segment counts, and a
-// checkpoint capacity for ck_mult * L / 33 starts.
+// checkpoint capacity (below).
+//
 // Candidates past its own end that a segment's truth range reaches before its
 // chain meets the next segment's (the link's walk): median ~130, 99th
 // percentile ~12000, largest seen ~15000 over random boundaries of the
@@ -307,7 +308,10 @@ void screen_shape(const csx_cfg &cfg, const csx_model &model, bool full, Plan *p
 // checkpoint a segment's final item grows instead (correct, but serial).
 constexpr uint64_t kLinkSlackCands = 24576;
 
-void segment_geometry(const csx_cfg &cfg, uint64_t seg, uint64_t ck_mult, StreamGeom &g) {
+// Checkpoints of a segment: one per D starts over `L / 33` starts (every
+// candidate 33 draws long), and with `slack` at least over the segment's
+// nominal candidates plus kLinkSlackCands.
+void segment_geometry(const csx_cfg &cfg, uint64_t seg, bool slack, StreamGeom &g) {
     const uint64_t my_max = std::max(g.per, g.my_last);
     const bool has_last = g.t0 + g.nT == g.T;
     // candidate length is constant when neither branch probability is mixed
@@ -321,8 +325,8 @@ void segment_geometry(const csx_cfg &cfg, uint64_t seg, uint64_t ck_mult, Stream
     g.C = static_cast<uint32_t>(std::max<uint64_t>(1, (64 * g.per + L - 1) / L));
     g.C_last = static_cast<uint32_t>(std::max<uint64_t>(1, (64 * g.my_last + L - 1) / L));
     g.n_seg = (g.nT - 1) * g.C + (has_last ? g.C_last : g.C);
-    uint64_t cover = ck_mult * L / 33;  // starts if every candidate were 33 draws long
-    if (ck_mult > 1) cover = std::max<uint64_t>(cover, std::min(seg, my_max) + kLinkSlackCands);
+    uint64_t cover = L / 33;  // starts if every candidate were 33 draws long
+    if (slack) cover = std::max<uint64_t>(cover, std::min(seg, my_max) + kLinkSlackCands);
     g.ckcap = static_cast<uint32_t>(cover / (1ull << g.d_log2) + 3);
 }
 
@@ -422,9 +426,11 @@ int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int
         const uint64_t sms = sharded ? kItemRefSms : static_cast<uint64_t>(cx.num_sms);
         seg = std::min<uint64_t>(kDefaultSegCands, std::max<uint64_t>(1024, lam_range / (256 * sms)));
     }
-    segment_geometry(cfg, seg, 2, g);
+    segment_geometry(cfg, seg, true, g);
     pl->short_path = my_max <= D;
-    pl->items_cap = pl->short_path ? g.nT : g.n_seg * (static_cast<uint64_t>(g.ckcap) + 1);
+    // a segment's range of cnt candidates splits at the multiples of D inside
+    // it: at most 2 + cnt / D items, and the ranges partition the candidates
+    pl->items_cap = pl->short_path ? g.nT : 2 * g.n_seg + lam_range / D + 1;
     if (pl->items_cap >= 0xFFFFFFFFull) return CSX_ERR_LIMIT;
     return CSX_OK;
 }
@@ -1144,12 +1150,12 @@ int noalloc_setup(int dev, NoAllocDevice **out) {
 // Plan for the fixed scratch: items of at least 16384 candidates (fewer items
 // and checkpoints). A segment's range of cnt candidates holds at most
 // ceil(cnt / D) split points, so items <= 2 * segments + lambda / D.
-// Checkpoints are sized for one segment's chain (ck_mult 1, where the pooled
-// plan takes 2): a link can land past its segment, and a checkpoint the walk
-// cannot store is dropped; split_range then clamps at the last stored one, so
-// that segment's last item grows instead (still within the items bound above)
-// and the result is unchanged. The pooled plan's margin buys smaller items,
-// which this plan does not need.
+// Checkpoints are sized for one segment's chain (no link margin, where the
+// pooled plan adds kLinkSlackCands): a link can land past its segment, and a
+// checkpoint the walk cannot store is dropped; split_range then clamps at the
+// last stored one, so that segment's last item grows instead (still within
+// the items bound above) and the result is unchanged. The pooled plan's margin
+// buys smaller items, which this plan does not need.
 int plan_noalloc(const NoAllocDevice &dv, const csx_cfg &cfg, const csx_model &model, int ne, Plan *pl) {
     StreamGeom &g = pl->g;
     int src = split_streams(cfg, 0, 0, g);
@@ -1167,7 +1173,7 @@ int plan_noalloc(const NoAllocDevice &dv, const csx_cfg &cfg, const csx_model &m
     while ((2ull << dl) <= d) ++dl;
     g.d_log2 = dl;
     const uint64_t D = 1ull << dl;
-    segment_geometry(cfg, kNoAllocSegCands, 1, g);
+    segment_geometry(cfg, kNoAllocSegCands, false, g);
     pl->short_path = my_max <= D;
     pl->items_cap = pl->short_path ? g.nT : 2 * g.n_seg + cfg.lambda / D + 1;
     if (pl->items_cap >= 0xFFFFFFFFull) return CSX_ERR_LIMIT;
