@@ -300,13 +300,15 @@ void screen_shape(const csx_cfg &cfg, const csx_model &model, bool full, Plan *p
 // checkpoint capacity (below).
 //
 // Candidates past its own end that a segment's truth range reaches before its
-// chain meets the next segment's (the link's walk): median ~130, 99th
-// percentile ~12000, largest seen ~15000 over random boundaries of the
-// reference's length rule (62 / 64 / 33 / 35 draws with immigrant 1%, jump
-// 2%). The pooled plan's checkpoints cover at least the segment plus this
-// margin, so short segments keep their items at D candidates; past the last
-// checkpoint a segment's final item grows instead (correct, but serial).
-constexpr uint64_t kLinkSlackCands = 24576;
+// chain meets the next segment's (the link's walk), simulated over 30000
+// random boundaries of the reference's length rule (62 / 64 / 33 / 35 draws,
+// immigrant 1%, jump 2%): median 136, 99th percentile 11.9k, 99.99th 24.1k,
+// largest 27.5k. The pooled plan's checkpoints cover at least the segment plus
+// this margin, so short segments keep their items at D candidates; past the
+// last checkpoint a segment's final item grows instead (correct, but one
+// thread screens it alone: a margin of 24576 left a few such items per island
+// of the batched workload and slowed it by a fifth).
+constexpr uint64_t kLinkSlackCands = 65536;
 
 // Checkpoints of a segment: one per D starts over `L / 33` starts (every
 // candidate 33 draws long), and with `slack` at least over the segment's
