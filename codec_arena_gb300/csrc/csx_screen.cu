@@ -414,6 +414,9 @@ int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int
         d = std::max<uint64_t>(1, lam_range / target);
         d = std::min<uint64_t>(16384, std::max<uint64_t>(64, d));
     }
+    // the link's speculative runs hold up to 32 starts and record at most one
+    // checkpoint each, so checkpoints (and items) stay at least 64 apart
+    d = std::max<uint64_t>(64, d);
     uint32_t dl = 0;
     while ((2ull << dl) <= d) ++dl;  // D = 2^dl <= d
     g.d_log2 = dl;

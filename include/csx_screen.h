@@ -258,7 +258,7 @@ int csx_last_run_info(csx_run_info *out);
  * Tunables do not change results, only speed (0 = automatic). */
 #define CSX_MAX_ISLANDS 64
 typedef struct csx_batch_tune {
-    uint32_t item_cands;  /* candidates per work item, rounded down to a power of two */
+    uint32_t item_cands;  /* candidates per work item, rounded down to a power of two, at least 64 */
     uint32_t seg_cands;   /* candidates per walk segment */
     uint32_t ctas_per_sm; /* persistent screen CTAs per SM (1..3) */
     uint32_t reserved;
