@@ -103,6 +103,27 @@ def test_pruned_and_unpruned_batch_forms_agree():
         _same(a, b)
 
 
+def test_pruned_batch_with_a_tail_surface(orc):
+    """One island's surface has large linear weights on genes 16..28, so its
+    pruning screen draws all 29 crossover bits, beside 16-bit islands and one
+    island with 256 elites (two CTAs per SM); every island equals the oracle."""
+    from codec_arena_gb300 import screen, islands, workloads as wl
+
+    rng = np.random.default_rng(12)
+    tail = rng.normal(0, 1, 166).astype(np.float32)
+    tail[17:30] = rng.normal(0, 20, 13).astype(np.float32)
+    ws = [tail, wl.surrogate_161(), wl.seeded_normal_model(seed=4)]
+    els = [wl.seeded_elites(64, 21), wl.seeded_elites(256, 22), wl.seeded_elites(7, 23)]
+    cfgs = [screen.Cfg(900_000, 64, 5, threads=4), screen.Cfg(1_200_000, 128, 6, threads=3),
+            screen.Cfg(400_000, 32, 7, threads=5, sigma=0.3)]
+    res = islands.screen_batch(cfgs, [screen.Model.from_compact(w) for w in ws], els)
+    for c, w, e, (surv, n) in zip(cfgs, ws, els, res):
+        oc = orc.cfg(c.lambda_, c.keep, c.seed, threads=c.threads, sigma=c.sigma)
+        want, wn = orc.screen(oc, orc.model_from_compact(w), e, cpu_threads=os.cpu_count() or 4)
+        assert n == wn == c.lambda_
+        _same(surv, want)
+
+
 def test_edge_islands():
     """Empty budget, budget below keep, two elites, keep 4096, one stream."""
     from codec_arena_gb300 import screen, islands, workloads as wl
