@@ -238,11 +238,18 @@ __device__ __forceinline__ float next_gene(GeneSource &S, int k) {
 // JumpBound::c[j], which the caller adds to the bound.
 // kJump: apply the jump (the exact form and kept genes always do; the filter
 // form leaves it out unless asked, as described above).
+// kGenes = 16: for a surface whose linear weights past gene 15 are all +-0,
+// genes 16..28 are not synthesised (their 26 draws skipped): each of their
+// terms is +-0 times a finite gene, the tail sum starts from +0 and so stays
+// +0, and the score is the lanes' sum + 0 either way. The jump's draws sit at
+// fixed offsets from the candidate's start (cand_head), so it applies as
+// before.
 template <bool kFastDelta, bool kKeepGenes, bool kExact = true, class Model = DevModel,
-          bool kJump = kExact || kKeepGenes>
+          bool kJump = kExact || kKeepGenes, int kGenes = kNtot>
 __device__ __forceinline__ float synth_score(const Model &M, const SynthConst &C,
                                              const float *__restrict__ el, uint64_t seed_t,
                                              uint64_t p, const CandHead &h, float *genes) {
+    static_assert(kGenes == kNtot || (kGenes == 16 && !kKeepGenes), "genes 16..28 are skipped only for a score");
     // next_gene's synthesis written out: through the helper the compiler
     // allocates this hot loop's registers differently (0.3% slower, measured)
     const uint64_t s0 = seed_t + (p + 1) * kGolden;
@@ -259,7 +266,7 @@ __device__ __forceinline__ float synth_score(const Model &M, const SynthConst &C
     float G[16], S[16];
     float R = kExact ? 0.0f : m_w16(M);
 #pragma unroll
-    for (int k = 0; k < kNtot; ++k) {
+    for (int k = 0; k < kGenes; ++k) {
         const uint32_t bw = draw_bitword(su - kGolden);  // crossover bit draw
         const uint32_t vh = draw_vh(su);                 // unit draw
         su += step;

@@ -75,11 +75,12 @@ __device__ void cta_sort_desc(Entry *E, uint32_t n) {
 // The reference-order score of one candidate, out of line: it runs only for
 // candidates the filter cannot rule out, and keeping it out of the caller
 // stops the compiler from holding both evaluations' values live at once.
-template <bool kFastDelta>
+// kGenes = 16 for a surface without linear weights past gene 15 (synth_score).
+template <bool kFastDelta, int kGenes = kNtot>
 __device__ __noinline__ float exact_score_at(const ScreenArgs *__restrict__ A, const float *el,
                                              uint64_t seed_t, uint64_t p) {
     const CandHead h = cand_head(A->sc, seed_t, p);
-    return synth_score<kFastDelta, false, true>(A->m, A->sc, el, seed_t, p, h, nullptr);
+    return synth_score<kFastDelta, false, true, DevModel, true, kGenes>(A->m, A->sc, el, seed_t, p, h, nullptr);
 }
 
 // The exact form (CSX_FLAG_EXACT_ALL, or a model whose filter bound is not
