@@ -361,6 +361,7 @@ RowModel make_row_model(const DevModel &m) {
     for (int k = 16; k < kNtot; ++k) r.v[kRowLin16 + k - 16] = m.wlin[k];
     r.v[kRowW16] = m.w16;
     r.v[kRowW16 + 1] = m.w0;
+    r.v[kRowW16 + 2] = m.tail ? 1.0f : 0.0f;
     return r;
 }
 

@@ -44,6 +44,7 @@ struct DevModel {
     float w16;  // 16 * w0 (exact): the intercept as Model.score counts it
     float wlin[kNtot];
     float wq[kNq];  // (i, j <= i) at i*(i+1)/2 + j  ==  Model.w_quad[i*16 + j]
+    uint32_t tail;  // some linear weight past gene 15 is nonzero (synth_score)
 };
 
 // Bound on how far a jump can raise the real score: with every gene in
@@ -77,7 +78,7 @@ __host__ __device__ constexpr int row_off(int k) {
     return o;
 }
 constexpr int kRowLin16 = row_off(16);      // 176
-constexpr int kRowW16 = kRowLin16 + 16;     // 192
+constexpr int kRowW16 = kRowLin16 + 16;     // 192: w16, w0, then the tail flag (1.0f / 0.0f)
 constexpr int kRowModelFloats = kRowW16 + 4;
 
 struct alignas(16) RowModel {
@@ -95,6 +96,8 @@ __device__ __forceinline__ float m_lin(const RowModel &M, int k) {
 }
 __device__ __forceinline__ float m_w0(const RowModel &M) { return M.v[kRowW16 + 1]; }
 __device__ __forceinline__ float m_w16(const RowModel &M) { return M.v[kRowW16]; }
+__device__ __forceinline__ bool m_tail(const DevModel &M) { return M.tail != 0u; }
+__device__ __forceinline__ bool m_tail(const RowModel &M) { return M.v[kRowW16 + 2] != 0.0f; }
 
 // y = z * kMix1 where z = s ^ (s >> 30): the first half of the mixer.
 __device__ __forceinline__ uint64_t mix_a(uint64_t s) {
@@ -238,18 +241,19 @@ __device__ __forceinline__ float next_gene(GeneSource &S, int k) {
 // JumpBound::c[j], which the caller adds to the bound.
 // kJump: apply the jump (the exact form and kept genes always do; the filter
 // form leaves it out unless asked, as described above).
-// kGenes = 16: for a surface whose linear weights past gene 15 are all +-0,
-// genes 16..28 are not synthesised (their 26 draws skipped): each of their
-// terms is +-0 times a finite gene, the tail sum starts from +0 and so stays
-// +0, and the score is the lanes' sum + 0 either way. The jump's draws sit at
-// fixed offsets from the candidate's start (cand_head), so it applies as
-// before.
+// kScoreOnly (the default without kept genes): for a surface whose linear
+// weights past gene 15 are all +-0 (m_tail false), genes 16..28 are not
+// synthesised (their 26 draws skipped): each of their terms is +-0 times a
+// finite gene, the tail sum starts from +0 and so stays +0, and the score is
+// the lanes' sum + 0 either way. The jump's draws sit at fixed offsets from
+// the candidate's start (cand_head), so it applies as before. With kept genes
+// and kScoreOnly, genes[16..28] are left as the caller set them.
 template <bool kFastDelta, bool kKeepGenes, bool kExact = true, class Model = DevModel,
-          bool kJump = kExact || kKeepGenes, int kGenes = kNtot>
+          bool kJump = kExact || kKeepGenes, bool kScoreOnly = !kKeepGenes>
 __device__ __forceinline__ float synth_score(const Model &M, const SynthConst &C,
                                              const float *__restrict__ el, uint64_t seed_t,
                                              uint64_t p, const CandHead &h, float *genes) {
-    static_assert(kGenes == kNtot || (kGenes == 16 && !kKeepGenes), "genes 16..28 are skipped only for a score");
+    const bool tail = !kScoreOnly || m_tail(M);
     // next_gene's synthesis written out: through the helper the compiler
     // allocates this hot loop's registers differently (0.3% slower, measured)
     const uint64_t s0 = seed_t + (p + 1) * kGolden;
@@ -266,7 +270,8 @@ __device__ __forceinline__ float synth_score(const Model &M, const SynthConst &C
     float G[16], S[16];
     float R = kExact ? 0.0f : m_w16(M);
 #pragma unroll
-    for (int k = 0; k < kGenes; ++k) {
+    for (int k = 0; k < kNtot; ++k) {
+        if (k == 16 && !tail) break;  // warp-uniform: one surface per call
         const uint32_t bw = draw_bitword(su - kGolden);  // crossover bit draw
         const uint32_t vh = draw_vh(su);                 // unit draw
         su += step;

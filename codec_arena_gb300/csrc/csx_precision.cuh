@@ -58,6 +58,8 @@ int make_tc_model(const csx_model &m, bool fp16, TcModel *t) {
             const int off = (n >> 3) * 256 + (k >> 3) * 128 + (n & 7) * 16 + (k & 7) * 2;
             t->btile[off / 2] = bits;
         }
+    t->tail = 0u;
+    for (int k = 16; k < kNtot; ++k) t->tail |= m.w_lin[k] != 0.0f ? 1u : 0u;
     return CSX_OK;
 }
 

@@ -146,13 +146,12 @@ __device__ __noinline__ float prune_rescore64(const ScreenArgs *__restrict__ A, 
     return static_cast<float>(score64_at<true>(&A->m, &A->sc, el, seed_t, p));  // out of line: own registers
 }
 
-// Score of a queued candidate: the reference's f32 order (out of line; genes
-// 0..15 only when kNb = 16, whose surface has no linear weight past them), or
+// Score of a queued candidate: the reference's f32 order (out of line), or
 // the precision form's FP64 score.
-template <bool kFp64, int kNb>
+template <bool kFp64>
 __device__ __forceinline__ float prune_rescore(const ScreenArgs *__restrict__ A, const float *el, uint64_t seed_t,
                                                uint64_t p, float tlo) {
-    if (!kFp64) return exact_score_at<true, kNb == 16 ? 16 : kNtot>(A, el, seed_t, p);
+    if (!kFp64) return exact_score_at<true>(A, el, seed_t, p);
     return prune_rescore64(A, el, seed_t, p, tlo);
 }
 
@@ -229,8 +228,7 @@ __global__ void __launch_bounds__(kThreads, 2) screen_p_kernel(const __grid_cons
 
     auto rescore = [&](const Pend &q, unsigned long long t1, unsigned long long t2, float ts) {
         const Item it = A.items[q.item];
-        const float s =
-            exact_score_at<true, kNb == 16 ? 16 : kNtot>(&A, el, stream_seed(A.seed, it.stream), it.draw0 + q.ddraw);
+        const float s = exact_score_at<true>(&A, el, stream_seed(A.seed, it.stream), it.draw0 + q.ddraw);
         ++exact;
         if (s >= ts) {
             const unsigned long long k1 =
@@ -477,7 +475,7 @@ __global__ void __launch_bounds__(kThreads, 3) screen_pt_kernel(const __grid_con
 
     auto rescore = [&](const Pend &q, unsigned long long t1, unsigned long long t2, float ts) {
         const Item it = A.items[q.item];
-        const float s = prune_rescore<kFp64, kNb>(&A, el, stream_seed(A.seed, it.stream), it.draw0 + q.ddraw,
+        const float s = prune_rescore<kFp64>(&A, el, stream_seed(A.seed, it.stream), it.draw0 + q.ddraw,
                                              __fsub_rd(ts, A.err));
         ++exact;
         if (s >= ts) {

@@ -461,6 +461,8 @@ DevModel make_dev_model(const csx_model &model) {
     for (int k = 0; k < kNtot; ++k) m.wlin[k] = model.w_lin[k];
     for (int i = 0; i < 16; ++i)
         for (int j = 0; j <= i; ++j) m.wq[tri(i, j)] = model.w_quad[i * 16 + j];
+    m.tail = 0u;
+    for (int k = 16; k < kNtot; ++k) m.tail |= model.w_lin[k] != 0.0f ? 1u : 0u;  // NaN counts as nonzero
     return m;
 }
 

@@ -75,12 +75,11 @@ __device__ void cta_sort_desc(Entry *E, uint32_t n) {
 // The reference-order score of one candidate, out of line: it runs only for
 // candidates the filter cannot rule out, and keeping it out of the caller
 // stops the compiler from holding both evaluations' values live at once.
-// kGenes = 16 for a surface without linear weights past gene 15 (synth_score).
-template <bool kFastDelta, int kGenes = kNtot>
+template <bool kFastDelta>
 __device__ __noinline__ float exact_score_at(const ScreenArgs *__restrict__ A, const float *el,
                                              uint64_t seed_t, uint64_t p) {
     const CandHead h = cand_head(A->sc, seed_t, p);
-    return synth_score<kFastDelta, false, true, DevModel, true, kGenes>(A->m, A->sc, el, seed_t, p, h, nullptr);
+    return synth_score<kFastDelta, false, true>(A->m, A->sc, el, seed_t, p, h, nullptr);
 }
 
 // The exact form (CSX_FLAG_EXACT_ALL, or a model whose filter bound is not
@@ -511,7 +510,9 @@ __device__ __noinline__ double score64_at(const DevModel *m, const SynthConst *s
                                           uint64_t p) {
     const CandHead h = cand_head(*sc, seed_t, p);
     float g[kNtot];
-    (void)synth_score<kFastDelta, true, true>(*m, *sc, el, seed_t, p, h, g);
+#pragma unroll
+    for (int k = 16; k < kNtot; ++k) g[k] = 0.0f;  // left so without a tail: weight +-0 times 0
+    (void)synth_score<kFastDelta, true, true, DevModel, true, true>(*m, *sc, el, seed_t, p, h, g);
     return score64_genes(*m, g);
 }
 

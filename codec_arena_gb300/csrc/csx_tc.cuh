@@ -35,6 +35,7 @@ struct TcModel {
     float c;
     float lin[kNtot];
     alignas(16) uint16_t btile[256];
+    uint32_t tail;  // some linear weight past gene 15 is nonzero (else genes 16..28 are skipped)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -188,6 +189,7 @@ __device__ __forceinline__ void synth_tc(const TcModel &T, const SynthConst &C, 
     R = T.c;
 #pragma unroll
     for (int k = 0; k < kNtot; ++k) {
+        if (k == 16 && !T.tail) break;  // no linear weight past gene 15: R gains +-0 from them
         const float g = next_gene<kFastDelta>(S, k);
         // no jump here: the caller lowers the threshold by JumpBound::c[h.jidx]
         R = __fmaf_rn(T.lin[k], g, R);
