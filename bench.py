@@ -52,23 +52,36 @@ KEEP = 256
 THREADS = 4
 SEED = 7
 N_ELITES = 64
-# Algorithmic 32-bit lane-ops per candidate of the full synthesis: 61.75
-# splitmix64 draws x 20 + 29 genes x 5 + 181 FMA x 2: the candidate's RNG, gene
-# arithmetic and scoring (the unpruned form).
-LANE_OPS_PER_CAND = 1760.0
-DRAWS_PER_CAND = 61.75
+# Algorithmic 32-bit lane-ops per candidate of the full synthesis and score
+# (the unpruned form's count, and the cost of each candidate queued for the
+# reference order): 61.75 splitmix64 draws x 20 + 29 genes x 5 + the score's
+# FMA x 2 = 1760 with a linear tail (weights on genes 16..28). Without one (the
+# committed v3 and the 153-term layouts) the score needs genes 0..15 only: the
+# tail's 0.99 x 26 crossover draws and 0.01 x 13 immigrant draws (x 20) and its
+# 13 genes (x 5) and 13 FMA (x 2) drop out: 1151.6.
+def full_synth_ops(tail):
+    if tail:
+        return 1760.0
+    return 1760.0 - (0.99 * 26 + 0.01 * 13) * 20 - 13 * (5 + 2)
+
+
 # The pruning form per candidate: the header's 4 draws (parents, immigrant
 # test, jump test) + 0.02 jump index draws, the 16 crossover-bit draws of the
 # 0.99 crossover candidates (x 20 lane-ops each), the bound's FP32 work on them
 # (4 x 16 lane-ops beside the tensor core's 16 x 16 MACs, 8 packs), and the
-# full 1760 for the fraction q queued for the reference-order score.
+# full synthesis for the fraction q queued for the reference-order score.
 PRUNE_DRAWS = 4.02 + 0.99 * 16
 PRUNE_FIXED_OPS = PRUNE_DRAWS * 20 + 0.99 * (4 * 16 + 8)
 PRUNE_TC_FLOP = 0.99 * 2 * 16 * 16  # tensor-core flops per candidate (the bound's gradient)
 
 
-def prune_ops(q):
-    return PRUNE_FIXED_OPS + q * LANE_OPS_PER_CAND
+def prune_ops(q, tail):
+    return PRUNE_FIXED_OPS + q * full_synth_ops(tail)
+
+
+def has_tail(model):
+    """Whether a surface (screen.Model) carries a linear weight on genes 16..28."""
+    return any(x != 0.0 for x in model.c.w_lin[16:29])
 
 
 def parse(argv=None):
@@ -921,7 +934,8 @@ def main():
     ms_screen = statistics.mean(screen_ms)
     cand_s_kernel = args.lam / (ms_screen / 1000.0)
     q = statistics.mean(st["exact_evals"] for st in stage) / args.lam  # queued for the reference order
-    ops = prune_ops(q)
+    tail = has_tail(model)
+    ops = prune_ops(q, tail)
     achieved = cand_s_kernel * ops / 1e12
     slots = issue_slots(achieved, clocks)
     prof = _profile_summary()
@@ -934,9 +948,10 @@ def main():
         "peak_source": slots.get("peak_source"),
         "algorithmic_ops_per_candidate": ops,
         "ops_model": ("pruning form: %.2f draws x 20 lane-ops (4 header draws, 0.02 jump index, 16 crossover "
-                      "bits for the 0.99 crossover candidates) + 0.99 x 72 bound lane-ops + q x 1760 for the "
-                      "fraction q queued for the full synthesis and reference-order score (measured q)"
-                      % PRUNE_DRAWS),
+                      "bits for the 0.99 crossover candidates) + 0.99 x 72 bound lane-ops + q x %.1f for the "
+                      "fraction q queued for the synthesis and reference-order score (measured q; %s)"
+                      % (PRUNE_DRAWS, full_synth_ops(tail),
+                         "genes 0..28" if tail else "genes 0..15: the surface has no linear weight past gene 15")),
         "queued_fraction": q,
         "traffic": traffic,
         "traffic_source": prof.get("traffic_note"),
@@ -980,8 +995,8 @@ def main():
         u = f["fp32_unpruned"]
         line["roofline"]["unpruned"] = {
             "kernel": "csx::screen_q_kernel<true>", "kernel_ms_per_launch": u["screen_kernel_ms"],
-            "algorithmic_ops_per_candidate": LANE_OPS_PER_CAND,
-            "issue_slots": issue_slots(args.lam / (u["screen_kernel_ms"] * 1e-3) * LANE_OPS_PER_CAND / 1e12,
+            "algorithmic_ops_per_candidate": full_synth_ops(tail),
+            "issue_slots": issue_slots(args.lam / (u["screen_kernel_ms"] * 1e-3) * full_synth_ops(tail) / 1e12,
                                        clocks)}
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args, args.cpu_seconds)
