@@ -421,15 +421,20 @@ int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int
     while ((2ull << dl) <= d) ++dl;  // D = 2^dl <= d
     g.d_log2 = dl;
     const uint64_t D = 1ull << dl;
-    // walk segments: kDefaultSegCands at large budgets; smaller budgets keep
-    // about 256 segments per SM down to 1024 candidates each, since the walk
-    // is serial within a segment (measured at lambda 1e6, T = 4: items 5.1 ms
-    // at 49152, 1.14 at 8192, 0.70 at 1024). Sharded calls size it by the
-    // fixed SM count, like the items.
+    // walk segments of about sqrt(lambda) candidates, within [1024, 49152]:
+    // the walk is serial within a segment (its time grows with the segment)
+    // and the link costs about the same per boundary (its total grows with
+    // lambda / segment), so the sum is least near sqrt(lambda) times a
+    // constant; measured optima: 1024 at 1e6 (items 0.70 ms, 5.1 at 49152),
+    // 12288 at 2e8 (2.56 ms; 3.47 at 5139, 5.68 at 49152), 49152 at 2.65e9.
+    // It depends on lambda only, so every share of a sharded call builds the
+    // same segments.
     uint64_t seg = seg_cands ? seg_cands : env_u64("CSX_SEG_CANDS", 0);
     if (seg == 0) {
-        const uint64_t sms = sharded ? kItemRefSms : static_cast<uint64_t>(cx.num_sms);
-        seg = std::min<uint64_t>(kDefaultSegCands, std::max<uint64_t>(1024, lam_range / (256 * sms)));
+        uint64_t r = static_cast<uint64_t>(std::sqrt(static_cast<double>(lam_range)));
+        while (r * r > lam_range) --r;
+        while ((r + 1) * (r + 1) <= lam_range) ++r;
+        seg = std::min<uint64_t>(kDefaultSegCands, std::max<uint64_t>(1024, r));
     }
     segment_geometry(cfg, seg, true, g);
     pl->short_path = my_max <= D;
