@@ -461,7 +461,8 @@ int batch_prepare(Context &cx, int n, const csx_cfg *cfgs, const csx_model *mode
         for (int i = 0; i < n; ++i) {
             if (cfgs[i].lambda == 0) continue;
             Plan &pl = L->pl[i];
-            pl.smem = prune_smem(pl.sort_n, n_elites[i], pl.nb, cx.num_sms, true);
+            pl.el_smem = prune_el_smem(pl.sort_n, n_elites[i], pl.nb, cx.num_sms, true, cx.max_smem);
+            pl.smem = prune_smem(pl.sort_n, n_elites[i], pl.nb, cx.num_sms, true, pl.el_smem);
             if (pl.smem + 1024 > cx.max_smem) return CSX_ERR_LIMIT;
             const int fit = std::min(cap, std::max(1, static_cast<int>((228u << 10) / (pl.smem + 1024))));
             pl.grid = fit * cx.num_sms;
@@ -574,6 +575,7 @@ int batch_prepare(Context &cx, int n, const csx_cfg *cfgs, const csx_model *mode
             P.tc = pl.ptc;
             P.pub = L->pub;
             P.sel_cap = 8u * static_cast<uint32_t>(cx.num_sms);
+            P.el_smem = pl.el_smem ? 1u : 0u;
         }
     }
     return CSX_OK;

@@ -65,6 +65,7 @@ struct PruneArgs : ScreenArgs {
     PruneTc tc;
     uint32_t *pub;     // kPruneMs x gridDim.x: okey of each CTA's 1st / 2nd / 4th best entry
     uint32_t sel_cap;  // entries of the selection scratch in shared memory (>= gridDim.x)
+    uint32_t el_smem;  // 1: the elite table is copied to shared memory (prune_el_smem)
 };
 
 // Row stride of the clamped parent table: odd, so that a warp reading random
@@ -182,8 +183,11 @@ __global__ void __launch_bounds__(kThreads, 2) screen_p_kernel(const __grid_cons
     constexpr int kYs = prune_stride<kNb>();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Entry *E = reinterpret_cast<Entry *>(smem_raw);
-    float *el = reinterpret_cast<float *>(E + A.sort_n);
-    Pend *pend = reinterpret_cast<Pend *>(el + (A.sc.ne + 1) * kNtot);
+    // the elite table: only the queued candidates' full synthesis reads it;
+    // in shared memory where that costs no CTA per SM, else through L1
+    float *el_copy = reinterpret_cast<float *>(E + A.sort_n);
+    const float *el = A.el_smem ? el_copy : A.el;
+    Pend *pend = reinterpret_cast<Pend *>(el_copy + (A.el_smem ? (A.sc.ne + 1) * kNtot : 0u));
     float *yt = reinterpret_cast<float *>(pend + kPendCap);
     uint32_t *sel = reinterpret_cast<uint32_t *>(yt + A.sc.ne * kYs);
     __shared__ unsigned int s_buf_n, s_pend_n;
@@ -192,7 +196,8 @@ __global__ void __launch_bounds__(kThreads, 2) screen_p_kernel(const __grid_cons
 
     const uint32_t tid = threadIdx.x;
     for (uint32_t i = tid; i < A.sort_n; i += kThreads) E[i] = Entry{0ull, 0ull};
-    for (uint32_t i = tid; i < (A.sc.ne + 1) * kNtot; i += kThreads) el[i] = A.el[i];
+    if (A.el_smem)
+        for (uint32_t i = tid; i < (A.sc.ne + 1) * kNtot; i += kThreads) el_copy[i] = A.el[i];
     for (uint32_t i = tid; i < A.sc.ne * kYs; i += kThreads) {
         const uint32_t r = i / kYs, k = i - r * kYs;
         // +inf (a NaN elite gene) clamps to 1, as the reference's clamp01(NaN + d)
@@ -402,8 +407,11 @@ __global__ void __launch_bounds__(kThreads, 3) screen_pt_kernel(const __grid_con
     constexpr int kYs = prune_stride<kNb>();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Entry *E = reinterpret_cast<Entry *>(smem_raw);
-    float *el = reinterpret_cast<float *>(E + A.sort_n);
-    Pend *pend = reinterpret_cast<Pend *>(el + (A.sc.ne + 1) * kNtot);
+    // the elite table: only the queued candidates' full synthesis reads it;
+    // in shared memory where that costs no CTA per SM, else through L1
+    float *el_copy = reinterpret_cast<float *>(E + A.sort_n);
+    const float *el = A.el_smem ? el_copy : A.el;
+    Pend *pend = reinterpret_cast<Pend *>(el_copy + (A.el_smem ? (A.sc.ne + 1) * kNtot : 0u));
     float *yt = reinterpret_cast<float *>(pend + kPendCap);
     uint32_t *sel = reinterpret_cast<uint32_t *>(yt + A.sc.ne * kYs);
     __shared__ __align__(8) unsigned long long s_mbar[2];
@@ -419,7 +427,8 @@ __global__ void __launch_bounds__(kThreads, 3) screen_pt_kernel(const __grid_con
     const uint32_t xs0 = (after + 1023u) & ~1023u;
     const uint32_t bts = xs0 + 2u * 4096u;
     for (uint32_t i = tid; i < A.sort_n; i += kThreads) E[i] = Entry{0ull, 0ull};
-    for (uint32_t i = tid; i < (A.sc.ne + 1) * kNtot; i += kThreads) el[i] = A.el[i];
+    if (A.el_smem)
+        for (uint32_t i = tid; i < (A.sc.ne + 1) * kNtot; i += kThreads) el_copy[i] = A.el[i];
     for (uint32_t i = tid; i < A.sc.ne * kYs; i += kThreads) {
         const uint32_t r = i / kYs, k = i - r * kYs;
         yt[i] = (k < static_cast<uint32_t>(kNb)) ? fmaxf(fminf(A.el[r * kNtot + k], 1.0f), 0.0f) : 0.0f;
@@ -648,15 +657,15 @@ PruneScreenFn screen_p_fn(int nb, bool tc, bool fp16, bool fp64) {
     return t ? screen_pt_kernel<kNtot, false, true> : screen_pt_kernel<16, false, true>;
 }
 
-// Shared memory of the pruning screen: the filter form's, the clamped parent
-// table and the selection scratch of the published keys (one per CTA, at
-// most 8 CTAs per SM); the tensor-core form adds its two X tiles and B tile
-// (1 KB aligned).
-size_t prune_smem(uint32_t sort_n, int ne, int nb, int num_sms, bool tc) {
+// Shared memory of the pruning screen: the sort buffer, the queue, the
+// clamped parent table and the selection scratch of the published keys (one
+// per CTA, at most 8 CTAs per SM), with el_smem the elite table; the
+// tensor-core form adds its two X tiles and B tile (1 KB aligned).
+size_t prune_smem(uint32_t sort_n, int ne, int nb, int num_sms, bool tc, bool el_smem) {
     const size_t ys = nb > 16 ? kNtot : 17;
-    const size_t n = static_cast<size_t>(sort_n) * sizeof(Entry) + static_cast<size_t>(ne + 1) * kNtot * sizeof(float) +
-                     kPendCap * sizeof(Pend) + static_cast<size_t>(ne) * ys * sizeof(float) +
-                     8ull * num_sms * sizeof(uint32_t);
+    const size_t n = static_cast<size_t>(sort_n) * sizeof(Entry) + kPendCap * sizeof(Pend) +
+                     static_cast<size_t>(ne) * ys * sizeof(float) + 8ull * num_sms * sizeof(uint32_t) +
+                     (el_smem ? static_cast<size_t>(ne + 1) * kNtot * sizeof(float) : 0);
     return tc ? n + 1024 + 2 * 4096 + 512 : n;
 }
 
@@ -765,6 +774,23 @@ bool make_prune_tc(const csx_model &m, const PruneConst &pc, bool fp16, PruneTc 
     t->c0 = c0 > 0.0 ? std::nextafter(static_cast<float>(c0), INFINITY) : 0.0f;
     t->err = std::nextafter(static_cast<float>(err), INFINITY);
     return true;
+}
+
+}  // namespace csx
+
+namespace csx {
+
+// CTAs per SM of a pruning screen with this shared memory (228 KB per SM, 1 KB
+// reserved per CTA; at most 3, the register limit of the tensor-core form).
+inline int prune_fit(size_t smem) { return std::min(3, static_cast<int>((228u << 10) / (smem + 1024))); }
+
+// Whether the elite table goes to shared memory: where it costs no CTA per SM
+// (the queue's synthesis reads it; through L1 it measured 0.7% slower at 64
+// elites, and at 256 elites the table would hold the screen to two CTAs per SM).
+inline bool prune_el_smem(uint32_t sort_n, int ne, int nb, int num_sms, bool tc, size_t max_smem) {
+    const size_t with = prune_smem(sort_n, ne, nb, num_sms, tc, true);
+    return with + 1024 <= max_smem &&
+           prune_fit(with) >= prune_fit(prune_smem(sort_n, ne, nb, num_sms, tc, false));
 }
 
 }  // namespace csx

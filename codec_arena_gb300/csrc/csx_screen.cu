@@ -149,6 +149,7 @@ struct Plan {
     bool prune_ok = false;  // its bound is certifiable for this call (the batch decides for itself)
     bool prune_tc = false;  // its bound's gradient on the tensor cores
     int nb = 16;            // crossover genes its bound draws
+    bool el_smem = false;   // its elite table in shared memory (prune_el_smem)
     PruneConst pc{};
     PruneTc ptc{};
 };
@@ -362,7 +363,8 @@ int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int
     pl->prune_ok = pl->prune;
     if (pl->prune && grid_override == 0) {
         // the selection scratch holds one key per CTA: at most 8 CTAs of 256 threads per SM
-        pl->smem = prune_smem(pl->sort_n, ne, pl->nb, cx.num_sms, pl->prune_tc);
+        pl->el_smem = prune_el_smem(pl->sort_n, ne, pl->nb, cx.num_sms, pl->prune_tc, cx.max_smem);
+        pl->smem = prune_smem(pl->sort_n, ne, pl->nb, cx.num_sms, pl->prune_tc, pl->el_smem);
         pl->prune = pl->smem + 1024 <= cx.max_smem;
     } else {
         pl->prune = false;
@@ -611,6 +613,7 @@ int enqueue_screen(Context &cx, const csx_cfg &cfg, const csx_model &model, cons
         P.tc = pl.ptc;
         P.pub = static_cast<uint32_t *>(cx.pub.p);
         P.sel_cap = 8u * static_cast<uint32_t>(cx.num_sms);
+        P.el_smem = pl.el_smem ? 1u : 0u;
         screen_p_fn(pl.nb, pl.prune_tc, pl.fp16 || !pl.tc, pl.tc)<<<pl.grid, kThreads, pl.smem, st>>>(P);
     } else if (pl.tc) {
         TcScreenArgs P;
