@@ -360,8 +360,15 @@ int make_plan(const Context &cx, const csx_cfg &cfg, const csx_model &model, int
     if (full && tcf) return CSX_ERR_BAD_ARGS;  // the precision form scores the reference surface
     pl->tc = tcf != 0;  // FP64 ranking (pruned, or the unpruned precision kernel)
     pl->fp16 = tcf == CSX_FLAG_TC_FP16;
-    pl->prune_ok = pl->prune;
-    if (pl->prune && grid_override == 0) {
+    // pruning pays once the generation gives each screen thread a few hundred
+    // candidates (the threshold then settles early; measured against the
+    // unpruned filter kernel: 0.40 against 0.29 ms at 1e6, 0.78 against 0.54
+    // at 1e7, 1.35 against 1.21 at 3e7, 3.14 against 3.45 at 1e8 candidates):
+    // prune from 400 per thread of a three-CTA-per-SM grid
+    const uint64_t sms = sharded ? kItemRefSms : static_cast<uint64_t>(cx.num_sms);
+    const uint64_t min_prune = env_u64("CSX_PRUNE_MIN_CANDS", 400ull * 3 * sms * kThreads);
+    pl->prune_ok = pl->prune && lam_range >= min_prune;
+    if (pl->prune_ok && grid_override == 0) {
         // the selection scratch holds one key per CTA: at most 8 CTAs of 256 threads per SM
         pl->el_smem = prune_el_smem(pl->sort_n, ne, pl->nb, cx.num_sms, pl->prune_tc, cx.max_smem);
         pl->smem = prune_smem(pl->sort_n, ne, pl->nb, cx.num_sms, pl->prune_tc, pl->el_smem);

@@ -7,6 +7,13 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
+# The library prunes only generations large enough for pruning to pay (about
+# 400 candidates per screen thread); the tests' generations are small, so they
+# lower that floor to 0 and run the pruning kernels at every size.
+# tests/test_gpu_screen.py::test_small_generations_take_the_unpruned_form
+# checks the automatic choice.
+os.environ.setdefault("CSX_PRUNE_MIN_CANDS", "0")
+
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA device (GB300)")

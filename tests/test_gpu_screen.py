@@ -471,3 +471,22 @@ def test_exact_ties_follow_the_reference_heap(orc, T, keep, lam):
         m = screen.Model.from_compact(w)
         parts = [screen.screen(cfg, m, el, streams=rg)[0] for rg in ((0, 1), (1, T))]
         assert parallel.merge_survivors(parts, keep).tobytes() == got.tobytes()
+
+
+def test_small_generations_take_the_unpruned_form(orc, env):
+    """Without the tests' floor the library screens a small generation with
+    the unpruned filter kernel (two CTAs per SM) and a large one with the
+    pruning screen (three); both equal the oracle."""
+    from codec_arena_gb300 import screen, workloads as wl
+
+    env.delenv("CSX_PRUNE_MIN_CANDS", raising=False)
+    w = wl.seeded_normal_model(seed=2)
+    el = wl.seeded_elites(64, seed=1)
+    got, n = screen.screen(screen.Cfg(1_000_000, 32, 7, threads=4), screen.Model.from_compact(w), el)
+    small = screen.last_run_info()
+    want, wn = orc.screen(orc.cfg(1_000_000, 32, 7, threads=4), orc.model_from_compact(w), el,
+                          cpu_threads=os.cpu_count() or 4)
+    assert n == wn and got.tobytes() == want.tobytes()
+    screen.screen(screen.Cfg(100_000_000, 32, 7, threads=4), screen.Model.from_compact(w), el)
+    large = screen.last_run_info()
+    assert small["screen_ctas"] < large["screen_ctas"], (small, large)
