@@ -67,7 +67,12 @@ enum {
 #define CSX_FLAG_NO_PRUNE 0x80u    /* score every candidate's full synthesis (the filter form)
                                       instead of skipping, by a certified bound taken after the
                                       crossover bits, candidates that cannot reach the top-K.
-                                      Results are identical either way; only speed differs */
+                                      Results are identical either way; only speed differs.
+                                      Without the flag the library prunes generations of at least
+                                      400 candidates per screen thread (3 CTAs x 256 threads per
+                                      SM: 4.67e7 on 152 SMs; below, the unpruned kernel is
+                                      faster); the environment variable CSX_PRUNE_MIN_CANDS sets
+                                      that floor in candidates */
 #define CSX_FLAG_PRUNE_FFMA 0x100u /* the pruning bound's gradient by FP32 FMA instead of the
                                       tensor cores (FP16 tcgen05.mma with a certified error
                                       share). Results are identical either way */
@@ -247,8 +252,9 @@ int csx_last_run_info(csx_run_info *out);
  * running brain/evolve.py with its own seed, elites and surrogate,
  * .github/workflows/arena.yml:56-92) in one pipeline: every island's work
  * items are built on its own forked stream; then, when every island's
- * surrogate admits the tensor-core pruning bound, each island's pruning
- * screen runs over the whole GPU in turn, else (or when any island carries
+ * surrogate admits the tensor-core pruning bound and every island is above
+ * the pruning floor (CSX_FLAG_NO_PRUNE), each island's pruning screen runs
+ * over the whole GPU in turn, else (or when any island carries
  * CSX_FLAG_NO_PRUNE) ONE unpruned persistent screen launch consumes all
  * islands' items and keeps a top-K per island; one merge tree and one
  * regeneration launch serve all islands. Results per island equal
