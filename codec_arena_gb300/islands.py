@@ -6,8 +6,9 @@ An island is what one CI shard of the reference runs each generation
 CUDA-graph launch of one pipeline and returns, per island, exactly what
 `screen.screen` returns for that island alone. The islands' item building runs
 on parallel streams; then, when every island's surrogate admits the pruning
-bound, each island's pruning screen runs in turn over the whole GPU, else one
-unpruned persistent screen kernel takes every island's candidates (a
+bound and every island is large enough for pruning to pay (the library's
+pruning floor), each island's pruning screen runs in turn over the whole GPU,
+else one unpruned persistent screen kernel takes every island's candidates (a
 FLAG_NO_PRUNE island selects that form for its batch). `Tune` holds the pipeline's tunables, which
 change speed only; `autotune` picks them by timing.
 """
