@@ -402,6 +402,46 @@ __device__ __forceinline__ void prune_parents(const PruneArgs &A, const float *_
 // precision form's ranking -- queued candidates are scored in FP64 and rank
 // by that score rounded to f32 (the FP64 top-K; PruneConst::err covers the
 // rounding of those scores too) -- instead of the reference's f32 order.
+// The tensor-core screen's merge, out of line (its sort keeps its registers
+// away from the screening loop's): the buffer into the CTA's sorted list, the
+// CTA threshold and its published order statistics, then (warp 0) the
+// threshold they certify. Every thread of the CTA calls it.
+__device__ __noinline__ void prune_merge(const PruneArgs *A, Entry *E, uint32_t *sel, unsigned int *s_buf_n,
+                                         unsigned long long *s_t1, unsigned long long *s_t2, float *s_ts) {
+    const uint32_t tid = threadIdx.x;
+    cta_sort_desc(E, A->sort_n);
+    for (uint32_t i = A->kpad + tid; i < A->sort_n; i += kThreads) E[i] = Entry{0ull, 0ull};
+    if (tid == 0) {
+        *s_buf_n = 0;
+        const Entry kth = E[A->keep - 1];
+        if (kth.k1 != 0ull) {
+            *s_t1 = kth.k1;
+            *s_t2 = kth.k2;
+            const unsigned int ok = static_cast<unsigned int>(kth.k1 >> 32);
+            *s_ts = okey_score(ok);
+            atomicMax(&A->ctrl->gtau, ok);
+        }
+    }
+    if (tid < kPruneMs && (1u << tid) <= A->keep) {
+        const unsigned int ok = static_cast<unsigned int>(E[(1u << tid) - 1].k1 >> 32);
+        if (ok != 0u) atomicMax(&A->pub[tid * gridDim.x + blockIdx.x], ok);
+    }
+    __syncthreads();
+    if (tid < 32) {
+        uint32_t best = 0;
+        for (int mi = 0; mi < kPruneMs; ++mi) {
+            const uint32_t jm = (A->keep + (1u << mi) - 1) >> mi;
+            if ((1u << mi) > A->keep || jm > gridDim.x) continue;
+            const volatile uint32_t *src = A->pub + mi * gridDim.x;
+            for (uint32_t i = tid; i < gridDim.x; i += 32) sel[i] = src[i];
+            __syncwarp();
+            best = max(best, warp_kth_largest(sel, gridDim.x, jm));
+            __syncwarp();
+        }
+        if (tid == 0 && best != 0u) atomicMax(&A->ctrl->gtau, best);
+    }
+}
+
 template <int kNb, bool kFp16, bool kFp64>
 __global__ void __launch_bounds__(kThreads, 3) screen_pt_kernel(const __grid_constant__ PruneArgs A) {
     constexpr int kYs = prune_stride<kNb>();
@@ -476,7 +516,7 @@ __global__ void __launch_bounds__(kThreads, 3) screen_pt_kernel(const __grid_con
         left = it.n;
         valid = left > 0;
     }
-    unsigned long long screened = 0, exact = 0;
+    uint32_t screened = 0, exact = 0;  // per thread: far below 2^32
     unsigned int gk = 0;
     uint32_t round = 0;
     bool has_def = false;
@@ -495,39 +535,7 @@ __global__ void __launch_bounds__(kThreads, 3) screen_pt_kernel(const __grid_con
         }
     };
 
-    auto merge = [&]() {
-        cta_sort_desc(E, A.sort_n);
-        for (uint32_t i = A.kpad + tid; i < A.sort_n; i += kThreads) E[i] = Entry{0ull, 0ull};
-        if (tid == 0) {
-            s_buf_n = 0;
-            const Entry kth = E[A.keep - 1];
-            if (kth.k1 != 0ull) {
-                s_t1 = kth.k1;
-                s_t2 = kth.k2;
-                const unsigned int ok = static_cast<unsigned int>(kth.k1 >> 32);
-                s_ts = okey_score(ok);
-                atomicMax(&A.ctrl->gtau, ok);
-            }
-        }
-        if (tid < kPruneMs && (1u << tid) <= A.keep) {
-            const unsigned int ok = static_cast<unsigned int>(E[(1u << tid) - 1].k1 >> 32);
-            if (ok != 0u) atomicMax(&A.pub[tid * gridDim.x + blockIdx.x], ok);
-        }
-        __syncthreads();
-        if (tid < 32) {
-            uint32_t best = 0;
-            for (int mi = 0; mi < kPruneMs; ++mi) {
-                const uint32_t jm = (A.keep + (1u << mi) - 1) >> mi;
-                if ((1u << mi) > A.keep || jm > gridDim.x) continue;
-                const volatile uint32_t *src = A.pub + mi * gridDim.x;
-                for (uint32_t i = tid; i < gridDim.x; i += 32) sel[i] = src[i];
-                __syncwarp();
-                best = max(best, warp_kth_largest(sel, gridDim.x, jm));
-                __syncwarp();
-            }
-            if (tid == 0 && best != 0u) atomicMax(&A.ctrl->gtau, best);
-        }
-    };
+    auto merge = [&]() { prune_merge(&A, E, sel, &s_buf_n, &s_t1, &s_t2, &s_ts); };
 
     for (;;) {
         __syncthreads();
@@ -627,13 +635,14 @@ __global__ void __launch_bounds__(kThreads, 3) screen_pt_kernel(const __grid_con
     }
     Entry *out = A.lists + static_cast<size_t>(blockIdx.x) * A.kpad;
     for (uint32_t i = tid; i < A.kpad; i += kThreads) out[i] = E[i];
+    unsigned long long scr = screened, exa = exact;
     for (int o = 16; o > 0; o >>= 1) {
-        screened += __shfl_down_sync(0xffffffffu, screened, o);
-        exact += __shfl_down_sync(0xffffffffu, exact, o);
+        scr += __shfl_down_sync(0xffffffffu, scr, o);
+        exa += __shfl_down_sync(0xffffffffu, exa, o);
     }
     if ((tid & 31) == 0) {
-        atomicAdd(&A.ctrl->screened, screened);
-        atomicAdd(&A.ctrl->exact_evals, exact);
+        atomicAdd(&A.ctrl->screened, scr);
+        atomicAdd(&A.ctrl->exact_evals, exa);
     }
     if (!tc_ok) atomicOr(&A.ctrl->err, kErrTc);
     __syncthreads();
