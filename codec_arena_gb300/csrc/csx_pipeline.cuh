@@ -149,27 +149,30 @@ __global__ void walk_kernel(SynthConst sc, StreamGeom g, SegRec *__restrict__ re
     const uint64_t b = static_cast<uint64_t>(c) * g.L, e = b + g.L;
     uint64_t *ckp = ck + s * g.ckcap;
     const uint32_t D = 1u << g.d_log2;
-    uint64_t p = b, k = 0;
+    // the position as the draws left to the segment end, a 32-bit count
+    // (segments are at most 2^30 draws: segment_geometry)
+    int32_t rem = static_cast<int32_t>(g.L);
+    uint64_t k = 0;
     uint64_t st = seed_t + (b + 1) * kGolden;
     const uint64_t limit = (ct == 1) ? my : ~0ull;  // a lone segment starts at the truth
-    while (p < e && k < limit) {
+    while (rem > 0 && k < limit) {
         const uint64_t m = k >> g.d_log2;  // k is a multiple of D here
-        if (m < g.ckcap) ckp[m] = p;
+        if (m < g.ckcap) ckp[m] = e - static_cast<uint64_t>(rem);
         const uint32_t n = static_cast<uint32_t>(min(static_cast<uint64_t>(D), limit - k));
         uint32_t j = 0;
         do {
             const uint32_t len = cand_len(sc, st);
-            p += len;
+            rem -= static_cast<int32_t>(len);
             st += static_cast<uint64_t>(len) * kGolden;
             ++j;
-        } while (j < n && p < e);
+        } while (j < n && rem > 0);
         k += j;
     }
     SegRec r;
     r.n = static_cast<uint32_t>(k);
     r.a = 0;
     r.b_next = 0;
-    r.merge_pos = p;  // the chain's first start at or past the segment end
+    r.merge_pos = e + static_cast<uint64_t>(-static_cast<int64_t>(rem));  // the first start at or past the end
     r.status = (c + 1 == ct) ? kSegLast : kSegOk;
     recs[s] = r;
 }

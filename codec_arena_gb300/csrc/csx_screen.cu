@@ -322,7 +322,7 @@ void segment_geometry(const csx_cfg &cfg, uint64_t seg, bool slack, StreamGeom &
     uint64_t gran = 2;
     if ((it == 0 || it == (1u << 24)) && (jt == 0 || jt == (1u << 24)))
         gran = (it ? 33 : 62) + (jt ? 2 : 0);
-    uint64_t L = 64 * std::min(seg, my_max);
+    uint64_t L = 64 * std::min(std::min<uint64_t>(seg, 1ull << 24), my_max);  // <= 2^30 draws (walk_kernel)
     L = ((L + gran - 1) / gran) * gran;
     g.L = L;
     g.C = static_cast<uint32_t>(std::max<uint64_t>(1, (64 * g.per + L - 1) / L));
