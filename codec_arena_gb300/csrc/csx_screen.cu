@@ -102,12 +102,15 @@ struct Context {
 
 Context g_ctx[64];
 
+// A decimal environment value, dflt when unset or not a number (an explicit 0
+// is 0: for CSX_ITEM_CANDS / CSX_SEG_CANDS that means automatic, for
+// CSX_PRUNE_MIN_CANDS prune at every size).
 uint64_t env_u64(const char *name, uint64_t dflt) {
     const char *v = std::getenv(name);
     if (!v || !*v) return dflt;
     char *end = nullptr;
     const unsigned long long x = std::strtoull(v, &end, 10);
-    return (end && *end == 0 && x > 0) ? x : dflt;
+    return (end && *end == 0) ? x : dflt;
 }
 
 uint32_t pow2_at_least(uint64_t x) {
