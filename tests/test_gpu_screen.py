@@ -476,12 +476,16 @@ def test_exact_ties_follow_the_reference_heap(orc, T, keep, lam):
 def test_small_generations_take_the_unpruned_form(orc, env):
     """Without the tests' floor the library screens a small generation with
     the unpruned filter kernel (two CTAs per SM) and a large one with the
-    pruning screen (three); both equal the oracle."""
+    pruning screen (three), which a floor of 0 selects at every size; the
+    small one equals the oracle."""
     from codec_arena_gb300 import screen, workloads as wl
 
-    env.delenv("CSX_PRUNE_MIN_CANDS", raising=False)
     w = wl.seeded_normal_model(seed=2)
     el = wl.seeded_elites(64, seed=1)
+    env.setenv("CSX_PRUNE_MIN_CANDS", "0")  # the tests' floor: prune at every size
+    screen.screen(screen.Cfg(1_000_000, 32, 7, threads=4), screen.Model.from_compact(w), el)
+    forced = screen.last_run_info()
+    env.delenv("CSX_PRUNE_MIN_CANDS", raising=False)
     got, n = screen.screen(screen.Cfg(1_000_000, 32, 7, threads=4), screen.Model.from_compact(w), el)
     small = screen.last_run_info()
     want, wn = orc.screen(orc.cfg(1_000_000, 32, 7, threads=4), orc.model_from_compact(w), el,
@@ -489,4 +493,4 @@ def test_small_generations_take_the_unpruned_form(orc, env):
     assert n == wn and got.tobytes() == want.tobytes()
     screen.screen(screen.Cfg(100_000_000, 32, 7, threads=4), screen.Model.from_compact(w), el)
     large = screen.last_run_info()
-    assert small["screen_ctas"] < large["screen_ctas"], (small, large)
+    assert small["screen_ctas"] < large["screen_ctas"] == forced["screen_ctas"], (small, large, forced)
