@@ -1,15 +1,21 @@
 // csx_batch.cuh — batched islands: many independent screens in one pipeline
-// and one persistent screen launch (csx_screen_batch, csx_screen_batch_device).
-// Part of csx_screen.cu's translation unit (included there, in order); not a
-// standalone header.
+// (csx_screen_batch, csx_screen_batch_device). Part of csx_screen.cu's
+// translation unit (included there, in order); not a standalone header.
 #pragma once
 
 // ---- batched islands -------------------------------------------------------------
 //
 // Several independent screens in one pipeline. Each island's items are built
 // by the single-screen stages on a forked stream of its own (the stages of
-// small islands are short of parallel work, so islands overlap). One
-// persistent launch then screens every island's items: a global counter hands
+// small islands are short of parallel work, so islands overlap). Then either
+// form screens them:
+//
+// * pruned (every island admits the tensor-core pruning bound and clears the
+//   pruning floor): each island's pruning screen (csx_prune.cuh) runs over the
+//   whole GPU in turn, with its own shared memory and grid, waiting only for
+//   its own island's items, and writes its CTA lists into the island's area;
+// * otherwise one persistent launch screens every island's items (below): a
+//   global counter hands
 // out items in island order, a thread whose next item belongs to a later
 // island parks it, and when no thread of the CTA has work left on the current
 // island the CTA publishes its top-K list for that island and switches to the
